@@ -1,0 +1,386 @@
+#!/usr/bin/env python3
+"""Throughput of the GB300 rasterisation path.
+
+Default workload: the single-large-mesh frame -- a displaced, textured
+icosphere of 1,310,720 triangles at 1920x1080 with near-plane clipping
+(minirender_gb300.workloads.config2).  One step = one complete frame through
+mr_render (clear, setup/clip/small-triangle raster, binning, tile raster,
+deferred resolve+shade to RGB8 and depth).
+
+  value   frames/s with the mesh and texture resident in HBM, device time of
+          K frames (CUDA events on the launching stream), L2 flushed between
+          frames by writing a 256 MiB buffer.
+  e2e     frames/s through the C ABI with host buffers: every step copies the
+          mesh and texture from pinned host memory (mr_mesh_update,
+          mr_texture_update), renders, and reads RGB8 + depth back.
+  --impl reference
+          the reference CPU algorithm (the oracle's C restatement; the
+          reference's own build needs ASL, which is unavailable) on all host
+          cores, one frame per thread per step.
+
+Multi-GPU (torchrun): independent replicas, one per rank, no collective on
+the data path; value = frames of all ranks / max over ranks of the time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "frames/s"
+UNIT = "frames/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="config2", choices=["config1", "config2", "config3"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_workload(name):
+    from minirender_gb300 import workloads as W
+    if name == "config1":
+        st, sc = W.config1()
+        desc = "uv-sphere 64x32 (3,968 tris), 640x480, point light, RGB8+depth"
+    elif name == "config3":
+        st, sc = W.config3()
+        desc = "10M-triangle soup (1-4 px^2, 5% exact duplicates), 3840x2160, palette texture"
+    else:
+        st, sc = W.config2()
+        desc = ("icosphere level 8 (1,310,720 tris) displaced by value noise, 1024^2 RGB8 "
+                "texture, near-plane clipping, 1920x1080, RGB8+depth")
+    return st, sc, desc
+
+
+class Clocks:
+    """nvidia-smi sampling thread for the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return ws, rank, local
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(workload: str):
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return {}
+    with open(p) as f:
+        return json.load(f).get(workload, {})
+
+
+def scene_sizes(sc):
+    from minirender_gb300 import scene as S
+    flat = S.flatten(sc)
+    V = sum(m.vertices.shape[0] for m in flat.meshes)
+    T = sum(m.n_triangles for m in flat.meshes)
+    mesh_bytes = sum(m.vertices.nbytes + m.normals.nbytes + m.texcoords.nbytes + 3 * m.indices.nbytes
+                     for m in flat.meshes)
+    tex_bytes = sum(t.nbytes for t in flat.textures)
+    return V, T, mesh_bytes, tex_bytes
+
+
+def cpu_frames_per_s(st, sc, n_threads: int, frames: int):
+    from oracle import oracle as O
+    O.build(with_ref=False)
+    secs = O.time_frames(st, sc, frames, n_threads)
+    return frames / secs, secs
+
+
+STAGES = ["clear", "setup", "bin", "tile_raster", "resolve"]
+KERNELS = {"clear": "k_clear", "setup": "k_setup", "bin": "k_bin_count+k_scan+k_bin_scatter",
+           "tile_raster": "k_tile_raster", "resolve": "k_resolve"}
+
+
+def gpu_arm(args, ws, rank, local):
+    import torch
+    from minirender_gb300 import abi, build
+    build.build()
+    from minirender_gb300.renderer import Renderer
+
+    torch.cuda.set_device(local)
+    st, sc, desc = make_workload(args.workload)
+    V, T, mesh_bytes, tex_bytes = scene_sizes(sc)
+    P = st.width * st.height
+    r = Renderer(local)
+    stream = torch.cuda.current_stream()
+    r.ctx.set_stream(stream.cuda_stream)
+    r.outputs = abi.MR_OUT_RGB8 | abi.MR_OUT_DEPTH
+    r.state = st
+    r.setScene(sc)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    frame, rs, n = r.prepare()
+    for _ in range(max(3, args.warmup)):
+        r.ctx.render(frame, rs, n, r.outputs)
+        r.ctx.stats()
+    r.ctx.synchronize()
+    r.ctx.set_profiling(True)
+    stage_tot = np.zeros(len(STAGES))
+    clocks = Clocks(local)
+    barrier(ws)
+    torch.cuda.synchronize()
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        r.ctx.render(frame, rs, n, r.outputs)
+        e1.record(stream)
+        s = r.ctx.stats()  # waits for the frame, reads per-stage event times
+        stage_tot += np.array(s.stage_ms[:len(STAGES)], np.float64)
+        step_ms.append(e0.elapsed_time(e1))
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    barrier(ws)
+    total_s = max_over_ranks(sum(step_ms) / 1e3, ws)
+    value = args.steps * ws / total_s
+    stats = r.ctx.stats()
+    r.ctx.set_profiling(False)
+
+    # ---- end to end through the C ABI, host buffers, copies inside the region
+    from minirender_gb300 import scene as S
+    flat = S.flatten(sc)
+    mesh = flat.meshes[0]
+    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    pm = S.TriMesh(pin(mesh.vertices), pin(mesh.normals), pin(mesh.indices), normalsI=pin(mesh.normalsI),
+                   texcoords=pin(mesh.texcoords) if mesh.texcoords.size else None,
+                   texcoordsI=pin(mesh.texcoordsI) if mesh.texcoordsI.size else None)
+    ptex = [pin(t) for t in flat.textures]
+    mh = r._meshes[id(mesh)][0]
+    th = [r._texture_handle(t) for t in flat.textures]
+    rgb8 = pin(np.empty((st.height, st.width, 3), np.uint8))
+    depth = pin(np.empty((st.height, st.width), np.float32))
+    h2d = mesh_bytes + tex_bytes
+    d2h = rgb8.nbytes + depth.nbytes
+
+    def e2e_step():
+        r.ctx.update_mesh(mh, pm.desc())
+        for h, t in zip(th, ptex):
+            r.ctx.update_texture(h, t)
+        r.ctx.render(frame, rs, n, r.outputs)
+        r.ctx.read_into(rgb8, depth)
+
+    for _ in range(2):
+        e2e_step()
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+    e2e_value = args.steps * ws / e2e_s
+    # resident variant: only the camera changes per frame
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.ctx.render(frame, rs, n, r.outputs)
+        r.ctx.read_into(rgb8, depth)
+    res_s = max_over_ranks(time.perf_counter() - t0, ws)
+
+    # ---- roofline of the dominant kernel
+    stage_ms = stage_tot / args.steps
+    dom = int(np.argmax(stage_ms))
+    name = STAGES[dom]
+    tex_px = P if flat.textures else 0
+    n_big = int(stats.binned)
+    alg = {
+        "clear": 8 * P,
+        "setup": 12 * T + 12 * V + 64 * n_big,
+        "bin": 2 * 64 * n_big + 8 * int(stats.bin_entries),
+        "tile_raster": 64 * int(stats.bin_entries),
+        "resolve": 8 * P + 7 * P + 3 * tex_px,
+    }
+    peak, peak_kind = peaks()
+    achieved = alg[name] / (stage_ms[dom] / 1e3) / 1e9
+    traffic = ncu_traffic(args.workload).get(KERNELS[name])
+    frame_bytes = 32 * V + 36 * T + 16 * P + 7 * P + 3 * tex_px
+    out = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(total_s * 1e3 / args.steps, 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": desc, "triangles": T, "vertices": V, "width": st.width,
+                   "height": st.height, "l2": "flushed between frames (256 MiB write)",
+                   "parallelism": "replicas" if ws > 1 else "single"},
+        "mtri_per_s": round(value * T / 1e6, 2),
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "e2e_resident_mesh": {"value": round(args.steps * ws / res_s, 3), "unit": UNIT,
+                              "h2d_bytes_per_step": 0, "d2h_bytes_per_step": int(d2h)},
+        "roofline": {"bound": "hbm", "kernel": KERNELS[name], "achieved": round(achieved, 2),
+                     "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "peak_source": peak_kind, "traffic": traffic,
+                     "algorithmic_bytes": int(alg[name]), "kernel_ms": round(float(stage_ms[dom]), 5)},
+        "stage_ms": {k: round(float(v), 5) for k, v in zip(STAGES, stage_ms)},
+        "frame_roofline": {"algorithmic_bytes": int(frame_bytes),
+                           "achieved_gbs": round(frame_bytes / (total_s / args.steps * ws) / 1e9, 2),
+                           "frac": round(frame_bytes / (total_s / args.steps * ws) / 1e9 / peak, 4)},
+        "counters": {"clipped": int(stats.clipped), "rasterised": int(stats.rasterised),
+                     "small_direct": int(stats.small_direct), "binned": int(stats.binned),
+                     "bin_entries": int(stats.bin_entries)},
+        "gpu_launches": 7 * args.steps,
+        "clocks": clk,
+    }
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        n_threads = os.cpu_count() or 1
+        frames = 2 * n_threads
+        fps, secs = cpu_frames_per_s(st, sc, n_threads, frames)
+        fps1, secs1 = cpu_frames_per_s(st, sc, 1, 1)
+        out["cpu_baseline"] = {
+            "value": round(fps, 4), "unit": UNIT, "cores": n_threads, "kind": "port",
+            "sample": f"{frames} frames of the same workload, one renderer per thread on "
+                      f"{n_threads} threads ({secs:.1f} s); single thread: {fps1:.4f} frames/s",
+            "single_thread_value": round(fps1, 4)}
+    r.close()
+    return out
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return None
+    st, sc, desc = make_workload(args.workload)
+    V, T, _, _ = scene_sizes(sc)
+    n_threads = os.cpu_count() or 1
+    for _ in range(max(0, args.warmup)):
+        pass  # the C restatement has no warm-up state; keep the loop shape
+    cpu_frames_per_s(st, sc, n_threads, n_threads)  # one untimed round (page-in)
+    total = 0.0
+    for _ in range(args.steps):
+        _, secs = cpu_frames_per_s(st, sc, n_threads, n_threads)
+        total += secs
+    value = args.steps * n_threads / total
+    return {
+        "metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(total * 1e3 / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator)", "impl": "reference",
+        "config": {"workload": desc, "triangles": T, "vertices": V, "width": st.width,
+                   "height": st.height, "parallelism": "host threads"},
+        "mtri_per_s": round(value * T / 1e6, 3),
+        "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": n_threads, "kind": "port",
+                         "sample": f"each step renders {n_threads} frames, one per host thread "
+                                   "(the reference's own build needs ASL, which is not available)"},
+        "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        out = reference_arm(args, ws, rank)
+    else:
+        out = gpu_arm(args, ws, rank, local)
+    if rank == 0 and out is not None:
+        print(json.dumps(out), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,220 @@
+/*
+ * minirender_gpu.h -- C ABI of the GB300 (sm_103a) rasterisation path that
+ * sits behind minirender's C++ Renderer.
+ *
+ * The reference exposes no C ABI: its interface is the C++ class
+ * minirender::Renderer (include/minirender/Renderer.h:17-64) fed by the scene
+ * model of include/minirender/Scene.h.  Each entry point below names the
+ * reference member or function whose work it takes over.  Plain pointers and
+ * sizes only; every call returns MR_OK (0) or a negative MR_E_* code, and
+ * mr_last_error() gives a one-line reason.
+ *
+ * Threading: a context may be shared between threads; calls on one context
+ * are serialised by an internal lock.  Device work is queued on the context's
+ * CUDA stream (mr_set_stream) and completes in call order.
+ *
+ * Numerics: all arithmetic is IEEE binary32 without fused multiply-add and in
+ * the reference's operation order, so coverage, depth and the visible
+ * triangle per pixel equal the reference CPU renderer bit for bit; colour may
+ * differ by rounding of powf/sqrtf/division only.
+ */
+#ifndef MINIRENDER_GPU_H
+#define MINIRENDER_GPU_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define MR_API __declspec(dllexport)
+#else
+#define MR_API __attribute__((visibility("default")))
+#endif
+
+#define MR_ABI_VERSION 1
+
+/* Status codes. */
+#define MR_OK 0
+#define MR_E_INVALID -1      /* bad argument or inconsistent sizes */
+#define MR_E_CUDA -2         /* a CUDA runtime call failed */
+#define MR_E_NOMEM -3        /* device allocation failed */
+#define MR_E_HANDLE -4       /* unknown mesh / texture / context handle */
+#define MR_E_BAD_INDEX -5    /* a mesh index was out of range (kernel-checked) */
+#define MR_E_BUDGET -6       /* request does not fit the device-memory budget */
+#define MR_E_TIMEOUT -7      /* a bounded device wait gave up */
+#define MR_E_NOT_READY -8    /* asynchronous result not available yet */
+#define MR_E_NO_DEVICE -9    /* no usable CUDA device */
+
+/* Background sentinel in the per-pixel triangle-id image. */
+#define MR_NO_TRIANGLE 0xFFFFFFFFu
+
+typedef struct mr_ctx mr_ctx;
+
+/* Material (include/minirender/Scene.h:38-45, defaults src/Scene.cpp:65-71).
+ * texture: handle from mr_texture_upload_* or -1 for none. */
+typedef struct mr_material {
+    float diffuse[3];
+    float specular[3];
+    float emissive[3];
+    float shininess;
+    int32_t texture;
+} mr_material;
+
+/* TriMesh arrays exactly as the reference holds them
+ * (include/minirender/Scene.h:73-87): Vec3 = 3 floats, Vec2 = 2 floats, one
+ * int per index.  n_* count elements (vertices, not floats).  texcoords are
+ * used only when both texcoords and texcoordsI are non-empty
+ * (src/Renderer.cpp:371). */
+typedef struct mr_mesh_desc {
+    const float* vertices;     int32_t n_vertices;
+    const float* normals;      int32_t n_normals;
+    const float* texcoords;    int32_t n_texcoords;
+    const int32_t* indices;    int32_t n_indices;
+    const int32_t* normalsI;   int32_t n_normalsI;
+    const int32_t* texcoordsI; int32_t n_texcoordsI;
+} mr_mesh_desc;
+
+/* One entry of Renderer::_renderables after Scene::collectShapes
+ * (include/minirender/Scene.h:47-53, src/Scene.cpp:13-36): the mesh, its
+ * world transform (row-major, m[4*i+j] = row i, column j) and the material
+ * paintMesh would use (mesh->material, or the default, src/Renderer.cpp:336). */
+typedef struct mr_renderable {
+    int32_t mesh;
+    int32_t reserved;
+    float transform[16];
+    mr_material material;
+} mr_renderable;
+
+/* Scene-graph node for mr_collect_shapes: nodes in pre-order, node 0 the
+ * root Scene, parent < own index.  mesh = -1 for a plain SceneNode. */
+typedef struct mr_node {
+    int32_t parent;
+    int32_t mesh;
+    float transform[16];
+    int32_t has_material;      /* 0: the Renderer's default material */
+    mr_material material;
+} mr_node;
+
+/* Renderer state read by Renderer::render() (src/Renderer.cpp:311-332). */
+typedef struct mr_frame {
+    int32_t width, height;          /* setSize */
+    float projection[16];           /* setProjection */
+    float view[16];                 /* setView */
+    float light[3];                 /* setLight */
+    int32_t light_is_point;
+    float ambient;                  /* Scene::ambientLight */
+    float background[3];            /* setBackground */
+    int32_t lighting;               /* setLighting */
+    int32_t texturing;              /* setTexturing */
+    int32_t save_normals;           /* setSaveNormals */
+} mr_frame;
+
+/* Device-side outputs of the last frame (device pointers, valid until the
+ * next mr_render on the context).  rgb8: H*W*3 bytes (savePPM quantisation,
+ * src/io.cpp:358-362); depth: H*W floats (getDepth); rgb_f32: H*W*3 floats
+ * (getImage), only when requested; tri_id: H*W u32 visible sub-triangle id
+ * 2*(global triangle index)+clip sub-triangle, MR_NO_TRIANGLE for
+ * background; normals: H*W*3 floats when save_normals. */
+typedef struct mr_outputs {
+    int32_t width, height;
+    uint8_t* rgb8;
+    float* depth;
+    float* rgb_f32;
+    uint32_t* tri_id;
+    float* normals;
+} mr_outputs;
+
+/* Output selection for mr_render (bit mask). */
+#define MR_OUT_RGB8    1
+#define MR_OUT_DEPTH   2
+#define MR_OUT_RGB_F32 4
+#define MR_OUT_TRI_ID  8
+#define MR_OUT_DEFAULT (MR_OUT_RGB8 | MR_OUT_DEPTH | MR_OUT_TRI_ID)
+
+/* Per-frame counters (device-side, read at the next synchronisation). */
+typedef struct mr_stats {
+    int64_t triangles;        /* submitted triangles */
+    int64_t clipped;          /* triangles that crossed the near plane */
+    int64_t rasterised;       /* sub-triangles past cull and reject */
+    int64_t small_direct;     /* rasterised in the setup kernel */
+    int64_t binned;           /* sub-triangles sent to tile bins */
+    int64_t bin_entries;      /* (tile, sub-triangle) pairs */
+    int64_t error_flags;      /* nonzero: MR_E_BAD_INDEX seen */
+    float stage_ms[8];        /* when profiling: clear, setup, bin, raster, resolve, ... */
+    int32_t n_stages;
+} mr_stats;
+
+/* ---- library / context --------------------------------------------- */
+MR_API int mr_abi_version(void);
+MR_API const char* mr_status_string(int status);
+MR_API const char* mr_last_error(const mr_ctx* ctx);
+
+/* Replaces: constructing a minirender::Renderer (src/Renderer.cpp:85-98). */
+MR_API int mr_create(int device, mr_ctx** out);
+MR_API int mr_destroy(mr_ctx* ctx);
+/* cudaStream_t passed as void*; NULL = the context's own stream. */
+MR_API int mr_set_stream(mr_ctx* ctx, void* cuda_stream);
+MR_API int mr_synchronize(mr_ctx* ctx);
+/* Tile edge (pixels, 8/16/32) and small-triangle bounding-box limit. */
+MR_API int mr_set_tuning(mr_ctx* ctx, int tile, int small_max);
+MR_API int mr_set_profiling(mr_ctx* ctx, int on);
+
+/* ---- resident data ----------------------------------------------------- */
+/* Replaces: the per-frame reads of TriMesh arrays in Renderer::paintMesh
+ * (src/Renderer.cpp:334-381); the mesh stays on the device. */
+MR_API int mr_mesh_upload(mr_ctx* ctx, const mr_mesh_desc* desc, int32_t* mesh_out);
+/* Re-copies the arrays of an existing mesh (same element counts). */
+MR_API int mr_mesh_update(mr_ctx* ctx, int32_t mesh, const mr_mesh_desc* desc);
+MR_API int mr_mesh_free(mr_ctx* ctx, int32_t mesh);
+/* Replaces: Material::texture filled by loadPPM (src/io.cpp:367-415): each
+ * texel is byte/255.0f, kept as RGB8 on the device. */
+MR_API int mr_texture_upload_rgb8(mr_ctx* ctx, const uint8_t* rgb, int32_t rows, int32_t cols,
+                                  int32_t* tex_out);
+/* Material::texture given as floats (Array2<Vec3>, row-major rows x cols x 3). */
+MR_API int mr_texture_upload_f32(mr_ctx* ctx, const float* rgb, int32_t rows, int32_t cols,
+                                 int32_t* tex_out);
+/* Re-copies the texels of an existing texture (same size and format). */
+MR_API int mr_texture_update(mr_ctx* ctx, int32_t tex, const void* texels);
+MR_API int mr_texture_free(mr_ctx* ctx, int32_t tex);
+
+/* ---- frame ------------------------------------------------------------- */
+/* Replaces: Renderer::render() after collectShapes (src/Renderer.cpp:311-332)
+ * with paintMesh/paintTriangle/clipTriangle (src/Renderer.cpp:121-381).
+ * Asynchronous: queued on the context stream. outputs: MR_OUT_* mask. */
+MR_API int mr_render(mr_ctx* ctx, const mr_frame* frame, const mr_renderable* renderables,
+                     int32_t n_renderables, int32_t outputs);
+/* Replaces: getImage/getDepth (include/minirender/Renderer.h:60-63) plus the
+ * savePPM byte conversion (src/io.cpp:358-362).  Copies the requested
+ * outputs of the last frame to host memory (NULL = skip) and waits. */
+MR_API int mr_read(mr_ctx* ctx, uint8_t* rgb8, float* depth, float* rgb_f32, uint32_t* tri_id,
+                   float* normals);
+MR_API int mr_get_outputs(mr_ctx* ctx, mr_outputs* out);
+MR_API int mr_get_stats(mr_ctx* ctx, mr_stats* out);
+/* Replaces: Renderer::getRangeImage (src/Renderer.cpp:388-415): view-space
+ * XYZ per pixel from the last depth buffer, H*W*3 floats to host memory. */
+MR_API int mr_read_range_image(mr_ctx* ctx, float* xyz);
+
+/* ---- host helpers (no device work) -------------------------------------- */
+/* Scene::collectShapes (src/Scene.cpp:13-36) over a pre-order node array.
+ * Writes at most cap renderables; *n_out = number produced. */
+MR_API int mr_collect_shapes(const mr_node* nodes, int32_t n_nodes, mr_renderable* out,
+                             int32_t cap, int32_t* n_out);
+/* Matrix4 product and inverse in the operation order the device path uses. */
+MR_API void mr_mat4_mul(const float* a, const float* b, float* out);
+MR_API void mr_mat4_inverse(const float* a, float* out);
+/* Projection builders (src/Renderer.cpp:40-83). */
+MR_API void mr_projection_ortho(float l, float r, float b, float t, float n, float f, float* out);
+MR_API void mr_projection_perspective(float l, float r, float b, float t, float n, float f,
+                                      float* out);
+MR_API void mr_projection_frustum(float fov, float aspect, float n, float f, float* out);
+MR_API void mr_projection_frustum_h(float fov, float aspect, float n, float f, float* out);
+MR_API void mr_projection_ortho_fov(float fov, float aspect, float n, float f, float* out);
+MR_API void mr_projection_cv(const float* K, float w, float h, float n, float f, float* out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MINIRENDER_GPU_H */

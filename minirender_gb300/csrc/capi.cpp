@@ -1,0 +1,650 @@
+// C ABI of the GB300 rasterisation path (include/minirender_gpu.h): context,
+// resident meshes/textures, per-frame staging and the launch sequence.
+//
+// Memory: the context owns every device buffer.  Meshes and textures are
+// allocated once at upload; frame buffers grow to the largest frame seen and
+// are then reused, so steady-state frames allocate nothing.  The one buffer
+// whose size is data dependent -- the (tile, triangle) bin list -- is
+// checked on the device; an overflow is detected at the next
+// synchronisation and the frame is re-run with a larger list.
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host_math.h"
+#include "layout.h"
+
+namespace mrg {
+cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st);
+cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev);
+cudaError_t launch_range(int W, int H, const float* dP, const float* depth, float* xyz,
+                         cudaStream_t st);
+}  // namespace mrg
+
+using namespace mrg;
+
+namespace {
+
+struct MeshRec {
+  bool live = false;
+  void* mem = nullptr;
+  DevMesh d{};
+  int32_t n_idx = 0;
+};
+
+struct TexRec {
+  bool live = false;
+  void* mem = nullptr;
+  bool rgb8 = false;
+  int32_t rows = 0, cols = 0;
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+struct mr_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  std::recursive_mutex mu;
+  std::vector<MeshRec> meshes;
+  std::vector<TexRec> textures;
+  DevBuf<unsigned long long> vis;
+  DevBuf<uint8_t> rgb8;
+  DevBuf<float> depth, rgbf, normals, range;
+  DevBuf<uint32_t> ids;
+  DevBuf<BigRec> recs;
+  DevBuf<uint32_t> bins;
+  DevBuf<uint32_t> tiles;
+  DevBuf<DevRenderable> rs;
+  DevBuf<uint32_t> tri_base;
+  DevBuf<float> dP;
+  DevRenderable* h_rs = nullptr;
+  size_t h_rs_cap = 0;
+  uint32_t* h_tri_base = nullptr;
+  Counters* d_cnt = nullptr;
+  Counters* h_cnt = nullptr;
+  cudaEvent_t ev[8] = {};
+  cudaEvent_t staged = nullptr;
+  bool profiling = false;
+  int tile = 16;
+  int small_max = 64;
+  bool have_frame = false;
+  bool pending = false;  // a frame was launched and not yet checked
+  FrameParams last{};
+  mr_frame last_frame{};
+  int outputs = 0;
+  std::string err;
+};
+
+static int fail(mr_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+static int cuda_fail(mr_ctx* c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(c, MR_E_NOMEM, m);
+  return fail(c, MR_E_CUDA, m);
+}
+
+#define CK(expr, what)                              \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
+  } while (0)
+
+extern "C" {
+
+MR_API int mr_abi_version(void) { return MR_ABI_VERSION; }
+
+MR_API const char* mr_status_string(int s) {
+  switch (s) {
+    case MR_OK: return "ok";
+    case MR_E_INVALID: return "invalid argument";
+    case MR_E_CUDA: return "CUDA error";
+    case MR_E_NOMEM: return "out of device memory";
+    case MR_E_HANDLE: return "unknown handle";
+    case MR_E_BAD_INDEX: return "mesh index out of range";
+    case MR_E_BUDGET: return "over device-memory budget";
+    case MR_E_TIMEOUT: return "device wait timed out";
+    case MR_E_NOT_READY: return "not ready";
+    case MR_E_NO_DEVICE: return "no CUDA device";
+    default: return "unknown status";
+  }
+}
+
+MR_API const char* mr_last_error(const mr_ctx* c) { return c ? c->err.c_str() : ""; }
+
+MR_API int mr_create(int device, mr_ctx** out) {
+  if (!out) return MR_E_INVALID;
+  *out = nullptr;
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess || n <= 0) {
+    cudaGetLastError();
+    return MR_E_NO_DEVICE;
+  }
+  if (device < 0 || device >= n) return MR_E_INVALID;
+  mr_ctx* c = new mr_ctx();
+  c->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaMalloc(&c->d_cnt, sizeof(Counters));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->h_cnt, sizeof(Counters));
+  for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = c->dP.ensure(16);
+  if (e != cudaSuccess) {
+    delete c;
+    return e == cudaErrorMemoryAllocation ? MR_E_NOMEM : MR_E_CUDA;
+  }
+  c->stream = c->own;
+  *out = c;
+  return MR_OK;
+}
+
+MR_API int mr_destroy(mr_ctx* c) {
+  if (!c) return MR_E_INVALID;
+  {
+    std::lock_guard<std::recursive_mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& m : c->meshes)
+      if (m.mem) cudaFree(m.mem);
+    for (auto& t : c->textures)
+      if (t.mem) cudaFree(t.mem);
+    c->vis.release(); c->rgb8.release(); c->depth.release(); c->rgbf.release();
+    c->normals.release(); c->range.release(); c->ids.release(); c->recs.release();
+    c->bins.release(); c->tiles.release(); c->rs.release(); c->tri_base.release(); c->dP.release();
+    if (c->h_rs) cudaFreeHost(c->h_rs);
+    if (c->h_tri_base) cudaFreeHost(c->h_tri_base);
+    if (c->d_cnt) cudaFree(c->d_cnt);
+    if (c->h_cnt) cudaFreeHost(c->h_cnt);
+    for (auto& e : c->ev)
+      if (e) cudaEventDestroy(e);
+    if (c->staged) cudaEventDestroy(c->staged);
+    if (c->own) cudaStreamDestroy(c->own);
+  }
+  delete c;
+  return MR_OK;
+}
+
+MR_API int mr_set_stream(mr_ctx* c, void* s) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  c->stream = s ? (cudaStream_t)s : c->own;
+  return MR_OK;
+}
+
+MR_API int mr_synchronize(mr_ctx* c) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
+  return MR_OK;
+}
+
+MR_API int mr_set_tuning(mr_ctx* c, int tile, int small_max) {
+  if (!c) return MR_E_INVALID;
+  if (tile != 8 && tile != 16 && tile != 32) return fail(c, MR_E_INVALID, "tile must be 8, 16 or 32");
+  if (small_max < 0 || small_max > 4096) return fail(c, MR_E_INVALID, "small_max out of range");
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  c->tile = tile;
+  c->small_max = small_max;
+  return MR_OK;
+}
+
+MR_API int mr_set_profiling(mr_ctx* c, int on) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  c->profiling = on != 0;
+  return MR_OK;
+}
+
+static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d) {
+  DevMesh& M = m.d;
+  char* base = (char*)m.mem;
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    char* p = base + off;
+    off += align256(bytes);
+    return (void*)p;
+  };
+  M.pos = (const float*)take((size_t)12 * d->n_vertices);
+  M.nrm = (const float*)take((size_t)12 * d->n_normals);
+  M.uv = (const float*)take((size_t)8 * (M.has_uv ? d->n_texcoords : 0));
+  M.idx = (const int32_t*)take((size_t)4 * d->n_indices);
+  M.nidx = (const int32_t*)take((size_t)4 * d->n_indices);
+  M.tidx = (const int32_t*)take((size_t)4 * (M.has_uv ? d->n_indices : 0));
+  M.bad = (const uint32_t*)take((size_t)4 * ((M.n_tri + 31) / 32 + 1));
+  cudaStream_t st = c->stream;
+  if (d->n_vertices) CK(cudaMemcpyAsync((void*)M.pos, d->vertices, (size_t)12 * d->n_vertices, cudaMemcpyHostToDevice, st), "mesh copy");
+  if (d->n_normals) CK(cudaMemcpyAsync((void*)M.nrm, d->normals, (size_t)12 * d->n_normals, cudaMemcpyHostToDevice, st), "mesh copy");
+  if (M.has_uv) CK(cudaMemcpyAsync((void*)M.uv, d->texcoords, (size_t)8 * d->n_texcoords, cudaMemcpyHostToDevice, st), "mesh copy");
+  if (d->n_indices) {
+    CK(cudaMemcpyAsync((void*)M.idx, d->indices, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
+    CK(cudaMemcpyAsync((void*)M.nidx, d->normalsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
+    if (M.has_uv) CK(cudaMemcpyAsync((void*)M.tidx, d->texcoordsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
+  }
+  CK(launch_validate(M, (uint32_t*)M.bad, st), "validate launch");
+  return MR_OK;
+}
+
+static int check_desc(mr_ctx* c, const mr_mesh_desc* d) {
+  if (!d) return fail(c, MR_E_INVALID, "null mesh descriptor");
+  if (d->n_vertices < 0 || d->n_normals < 0 || d->n_texcoords < 0 || d->n_indices < 0 ||
+      d->n_normalsI < 0 || d->n_texcoordsI < 0)
+    return fail(c, MR_E_INVALID, "negative count");
+  if (d->n_indices % 3) return fail(c, MR_E_INVALID, "index count is not a multiple of 3");
+  if (d->n_normalsI < d->n_indices) return fail(c, MR_E_INVALID, "normalsI shorter than indices");
+  bool has_uv = d->n_texcoords > 0 && d->n_texcoordsI > 0;
+  if (has_uv && d->n_texcoordsI < d->n_indices)
+    return fail(c, MR_E_INVALID, "texcoordsI shorter than indices");
+  if ((d->n_vertices && !d->vertices) || (d->n_normals && !d->normals) ||
+      (has_uv && (!d->texcoords || !d->texcoordsI)) || (d->n_indices && (!d->indices || !d->normalsI)))
+    return fail(c, MR_E_INVALID, "null array with non-zero count");
+  return MR_OK;
+}
+
+static size_t mesh_bytes(const mr_mesh_desc* d, bool has_uv) {
+  int ntri = d->n_indices / 3;
+  return align256((size_t)12 * d->n_vertices) + align256((size_t)12 * d->n_normals) +
+         align256((size_t)8 * (has_uv ? d->n_texcoords : 0)) + 2 * align256((size_t)4 * d->n_indices) +
+         align256((size_t)4 * (has_uv ? d->n_indices : 0)) + align256((size_t)4 * ((ntri + 31) / 32 + 1));
+}
+
+MR_API int mr_mesh_upload(mr_ctx* c, const mr_mesh_desc* d, int32_t* out) {
+  if (!c || !out) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  int rc = check_desc(c, d);
+  if (rc) return rc;
+  cudaSetDevice(c->device);
+  MeshRec m;
+  m.live = true;
+  m.n_idx = d->n_indices;
+  m.d.has_uv = d->n_texcoords > 0 && d->n_texcoordsI > 0;
+  m.d.n_pos = d->n_vertices;
+  m.d.n_nrm = d->n_normals;
+  m.d.n_uv = m.d.has_uv ? d->n_texcoords : 0;
+  m.d.n_tri = d->n_indices / 3;
+  CK(cudaMalloc(&m.mem, mesh_bytes(d, m.d.has_uv)), "mesh allocation");
+  rc = copy_mesh(c, m, d);
+  if (rc) {
+    cudaFree(m.mem);
+    return rc;
+  }
+  int32_t h = -1;
+  for (size_t i = 0; i < c->meshes.size(); i++)
+    if (!c->meshes[i].live) { h = (int32_t)i; break; }
+  if (h < 0) {
+    h = (int32_t)c->meshes.size();
+    c->meshes.push_back(m);
+  } else {
+    c->meshes[h] = m;
+  }
+  *out = h;
+  return MR_OK;
+}
+
+MR_API int mr_mesh_update(mr_ctx* c, int32_t h, const mr_mesh_desc* d) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  if (h < 0 || h >= (int32_t)c->meshes.size() || !c->meshes[h].live) return fail(c, MR_E_HANDLE, "unknown mesh");
+  int rc = check_desc(c, d);
+  if (rc) return rc;
+  MeshRec& m = c->meshes[h];
+  bool has_uv = d->n_texcoords > 0 && d->n_texcoordsI > 0;
+  if (d->n_vertices != m.d.n_pos || d->n_normals != m.d.n_nrm || d->n_indices != m.n_idx ||
+      has_uv != (m.d.has_uv != 0) || (has_uv && d->n_texcoords != m.d.n_uv))
+    return fail(c, MR_E_INVALID, "mr_mesh_update needs the same element counts");
+  cudaSetDevice(c->device);
+  return copy_mesh(c, m, d);
+}
+
+MR_API int mr_mesh_free(mr_ctx* c, int32_t h) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  if (h < 0 || h >= (int32_t)c->meshes.size() || !c->meshes[h].live) return fail(c, MR_E_HANDLE, "unknown mesh");
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->meshes[h].mem);
+  c->meshes[h] = MeshRec();
+  return MR_OK;
+}
+
+static int tex_upload(mr_ctx* c, const void* data, size_t bytes, bool rgb8, int32_t rows, int32_t cols,
+                      int32_t* out) {
+  if (!c || !out || !data || rows <= 0 || cols <= 0) return fail(c, MR_E_INVALID, "bad texture");
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  TexRec t;
+  t.live = true;
+  t.rgb8 = rgb8;
+  t.rows = rows;
+  t.cols = cols;
+  CK(cudaMalloc(&t.mem, bytes), "texture allocation");
+  cudaError_t e = cudaMemcpyAsync(t.mem, data, bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e != cudaSuccess) {
+    cudaFree(t.mem);
+    return cuda_fail(c, e, "texture copy");
+  }
+  int32_t h = -1;
+  for (size_t i = 0; i < c->textures.size(); i++)
+    if (!c->textures[i].live) { h = (int32_t)i; break; }
+  if (h < 0) {
+    h = (int32_t)c->textures.size();
+    c->textures.push_back(t);
+  } else {
+    c->textures[h] = t;
+  }
+  *out = h;
+  return MR_OK;
+}
+
+MR_API int mr_texture_upload_rgb8(mr_ctx* c, const uint8_t* rgb, int32_t rows, int32_t cols, int32_t* out) {
+  return tex_upload(c, rgb, (size_t)3 * rows * cols, true, rows, cols, out);
+}
+
+MR_API int mr_texture_upload_f32(mr_ctx* c, const float* rgb, int32_t rows, int32_t cols, int32_t* out) {
+  return tex_upload(c, rgb, (size_t)12 * rows * cols, false, rows, cols, out);
+}
+
+MR_API int mr_texture_update(mr_ctx* c, int32_t h, const void* texels) {
+  if (!c || !texels) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  if (h < 0 || h >= (int32_t)c->textures.size() || !c->textures[h].live) return fail(c, MR_E_HANDLE, "unknown texture");
+  const TexRec& t = c->textures[h];
+  size_t bytes = (size_t)t.rows * t.cols * (t.rgb8 ? 3 : 12);
+  cudaSetDevice(c->device);
+  CK(cudaMemcpyAsync(t.mem, texels, bytes, cudaMemcpyHostToDevice, c->stream), "texture copy");
+  return MR_OK;
+}
+
+MR_API int mr_texture_free(mr_ctx* c, int32_t h) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  if (h < 0 || h >= (int32_t)c->textures.size() || !c->textures[h].live) return fail(c, MR_E_HANDLE, "unknown texture");
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  cudaFree(c->textures[h].mem);
+  c->textures[h] = TexRec();
+  return MR_OK;
+}
+
+// Launches the kernels of c->last after resetting the per-frame counters.
+static int launch_last(mr_ctx* c) {
+  FrameParams& F = c->last;
+  cudaStream_t st = c->stream;
+  int ntiles = F.tiles_x * F.tiles_y;
+  CK(cudaMemsetAsync(c->d_cnt, 0, sizeof(Counters), st), "counter reset");
+  CK(cudaMemsetAsync(c->tiles.p, 0, sizeof(uint32_t) * (size_t)(3 * ntiles + 1), st), "tile reset");
+  CK(launch_frame(F, st, c->profiling ? c->ev : nullptr), "frame launch");
+  return MR_OK;
+}
+
+MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int32_t n, int32_t outputs) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  if (!f || (n > 0 && !rs) || n < 0) return fail(c, MR_E_INVALID, "null frame or renderables");
+  if (f->width <= 0 || f->height <= 0 || (int64_t)f->width * f->height > (int64_t)1 << 28 ||
+      f->width > (1 << 16) || f->height > (1 << 16))
+    return fail(c, MR_E_INVALID, "frame size out of range");
+  cudaSetDevice(c->device);
+  // Per-renderable matrices and materials, Renderer::paintMesh (src/Renderer.cpp:336-338).
+  uint64_t total = 0;
+  for (int32_t i = 0; i < n; i++) {
+    int32_t h = rs[i].mesh;
+    if (h < 0 || h >= (int32_t)c->meshes.size() || !c->meshes[h].live)
+      return fail(c, MR_E_HANDLE, "renderable refers to an unknown mesh");
+    int32_t t = rs[i].material.texture;
+    if (t >= 0 && (t >= (int32_t)c->textures.size() || !c->textures[t].live))
+      return fail(c, MR_E_HANDLE, "material refers to an unknown texture");
+    total += (uint64_t)c->meshes[h].d.n_tri;
+  }
+  if (total >= ((uint64_t)1 << 31)) return fail(c, MR_E_INVALID, "more than 2^31-1 triangles in one frame");
+  size_t nrs = (size_t)std::max(n, 1);
+  if (c->h_rs_cap < nrs) {
+    CK(cudaEventSynchronize(c->staged), "staging wait");
+    if (c->h_rs) cudaFreeHost(c->h_rs);
+    if (c->h_tri_base) cudaFreeHost(c->h_tri_base);
+    c->h_rs = nullptr;
+    c->h_tri_base = nullptr;
+    c->h_rs_cap = 0;
+    CK(cudaMallocHost(&c->h_rs, sizeof(DevRenderable) * nrs), "pinned staging");
+    CK(cudaMallocHost(&c->h_tri_base, sizeof(uint32_t) * (nrs + 1)), "pinned staging");
+    c->h_rs_cap = nrs;
+  } else {
+    CK(cudaEventSynchronize(c->staged), "staging wait");
+  }
+  uint32_t base = 0;
+  for (int32_t i = 0; i < n; i++) {
+    const MeshRec& m = c->meshes[rs[i].mesh];
+    DevRenderable& R = c->h_rs[i];
+    float mv[16], inv[16], nm[16];
+    mat4_mul(f->view, rs[i].transform, mv);
+    mat4_inverse(mv, inv);
+    mat4_transpose(inv, nm);
+    memcpy(R.mv, mv, sizeof(R.mv));
+    memcpy(R.nm, nm, sizeof(R.nm));
+    R.mesh = m.d;
+    R.tri_base = base;
+    c->h_tri_base[i] = base;
+    base += (uint32_t)m.d.n_tri;
+    const mr_material& M = rs[i].material;
+    memcpy(R.diffuse, M.diffuse, sizeof(R.diffuse));
+    memcpy(R.specular, M.specular, sizeof(R.specular));
+    memcpy(R.emissive, M.emissive, sizeof(R.emissive));
+    R.shininess = M.shininess;
+    R.has_tex = 0;
+    R.tex8 = nullptr;
+    R.texf = nullptr;
+    R.tex_rows = R.tex_cols = 0;
+    if (f->texturing && M.texture >= 0) {
+      const TexRec& T = c->textures[M.texture];
+      R.has_tex = 1;
+      R.tex_rows = T.rows;
+      R.tex_cols = T.cols;
+      if (T.rgb8) R.tex8 = (const uint8_t*)T.mem;
+      else R.texf = (const float*)T.mem;
+    }
+  }
+  c->h_tri_base[n] = base;
+
+  const int W = f->width, H = f->height;
+  const size_t npx = (size_t)W * H;
+  const int TS = c->tile;
+  const int tx = (W + TS - 1) / TS, ty = (H + TS - 1) / TS;
+  CK(c->vis.ensure(npx), "vis buffer");
+  if (outputs & MR_OUT_RGB8) CK(c->rgb8.ensure(3 * npx), "rgb8 buffer");
+  if (outputs & MR_OUT_DEPTH) CK(c->depth.ensure(npx), "depth buffer");
+  if (outputs & MR_OUT_RGB_F32) CK(c->rgbf.ensure(3 * npx), "rgb buffer");
+  if (outputs & MR_OUT_TRI_ID) CK(c->ids.ensure(npx), "id buffer");
+  if (f->save_normals) CK(c->normals.ensure(3 * npx), "normals buffer");
+  CK(c->recs.ensure((size_t)2 * total), "record buffer");
+  CK(c->tiles.ensure((size_t)3 * tx * ty + 1), "tile buffer");
+  if (c->bins.cap < ((size_t)1 << 20)) CK(c->bins.ensure((size_t)1 << 20), "bin buffer");
+  CK(c->rs.ensure(nrs), "renderable table");
+  CK(c->tri_base.ensure(nrs + 1), "triangle base table");
+  CK(cudaMemcpyAsync(c->rs.p, c->h_rs, sizeof(DevRenderable) * n, cudaMemcpyHostToDevice, c->stream), "renderable upload");
+  CK(cudaMemcpyAsync(c->tri_base.p, c->h_tri_base, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, c->stream), "base upload");
+  CK(cudaMemcpyAsync(c->dP.p, f->projection, sizeof(float) * 16, cudaMemcpyHostToDevice, c->stream), "projection upload");
+  CK(cudaEventRecord(c->staged, c->stream), "staging event");
+
+  FrameParams& F = c->last;
+  memset(&F, 0, sizeof(F));
+  F.W = W;
+  F.H = H;
+  F.w = (float)W;
+  F.h = (float)H;
+  memcpy(F.P, f->projection, sizeof(F.P));
+  // Renderer::render, src/Renderer.cpp:317-326.
+  F.persp = f->projection[15] == 0;
+  float zn = F.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
+  F.znear = -zn;
+  F.point = f->light_is_point != 0;
+  if (F.point) affine(f->view, f->light, F.lightdir);
+  else normalized(f->light, F.lightdir);
+  F.ambient = f->ambient;
+  F.lighting = f->lighting != 0;
+  F.save_normals = f->save_normals != 0;
+  memcpy(F.bg, f->background, sizeof(F.bg));
+  F.n_renderables = n;
+  F.n_tris = (uint32_t)total;
+  F.tile = TS;
+  F.tiles_x = tx;
+  F.tiles_y = ty;
+  F.small_max = c->small_max;
+  F.rs = c->rs.p;
+  F.tri_base = c->tri_base.p;
+  F.vis = c->vis.p;
+  F.recs = c->recs.p;
+  F.rec_cap = (uint32_t)std::min<size_t>(c->recs.cap, 0xFFFFFFFFu);
+  F.tile_count = c->tiles.p;
+  F.tile_fill = c->tiles.p + (size_t)tx * ty;
+  F.tile_start = c->tiles.p + (size_t)2 * tx * ty;
+  F.bins = c->bins.p;
+  F.bin_cap = (uint32_t)std::min<size_t>(c->bins.cap, 0xFFFFFFFFu);
+  F.rgb8 = (outputs & MR_OUT_RGB8) ? c->rgb8.p : nullptr;
+  F.depth = (outputs & MR_OUT_DEPTH) ? c->depth.p : nullptr;
+  F.rgbf = (outputs & MR_OUT_RGB_F32) ? c->rgbf.p : nullptr;
+  F.ids = (outputs & MR_OUT_TRI_ID) ? c->ids.p : nullptr;
+  F.normals = f->save_normals ? c->normals.p : nullptr;
+  F.counters = c->d_cnt;
+  c->last_frame = *f;
+  c->outputs = outputs;
+  c->have_frame = true;
+  c->pending = true;
+  return launch_last(c);
+}
+
+// Waits for the last frame; re-runs it while the bin list overflowed.
+static int settle(mr_ctx* c) {
+  if (!c->have_frame) return fail(c, MR_E_INVALID, "no frame rendered yet");
+  for (int attempt = 0; attempt < 8; attempt++) {
+    CK(cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "counter read");
+    CK(cudaStreamSynchronize(c->stream), "frame wait");
+    if (!c->h_cnt->bin_overflow) {
+      c->pending = false;
+      return (c->h_cnt->error_flags & 1u) ? fail(c, MR_E_BAD_INDEX, "a mesh index was out of range; those triangles were skipped") : MR_OK;
+    }
+    size_t want = (size_t)c->h_cnt->bin_needed + c->h_cnt->bin_needed / 4 + 1024;
+    CK(c->bins.ensure(want), "bin buffer");
+    c->last.bins = c->bins.p;
+    c->last.bin_cap = (uint32_t)std::min<size_t>(c->bins.cap, 0xFFFFFFFFu);
+    int rc = launch_last(c);
+    if (rc) return rc;
+  }
+  return fail(c, MR_E_NOMEM, "bin list kept overflowing");
+}
+
+MR_API int mr_read(mr_ctx* c, uint8_t* rgb8, float* depth, float* rgb_f32, uint32_t* tri_id, float* normals) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  int rc = settle(c);
+  if (rc && rc != MR_E_BAD_INDEX) return rc;
+  size_t npx = (size_t)c->last.W * c->last.H;
+  cudaStream_t st = c->stream;
+  if (rgb8) {
+    if (!c->last.rgb8) return fail(c, MR_E_INVALID, "rgb8 was not requested for this frame");
+    CK(cudaMemcpyAsync(rgb8, c->last.rgb8, 3 * npx, cudaMemcpyDeviceToHost, st), "rgb8 read");
+  }
+  if (depth) {
+    if (!c->last.depth) return fail(c, MR_E_INVALID, "depth was not requested for this frame");
+    CK(cudaMemcpyAsync(depth, c->last.depth, 4 * npx, cudaMemcpyDeviceToHost, st), "depth read");
+  }
+  if (rgb_f32) {
+    if (!c->last.rgbf) return fail(c, MR_E_INVALID, "float image was not requested for this frame");
+    CK(cudaMemcpyAsync(rgb_f32, c->last.rgbf, 12 * npx, cudaMemcpyDeviceToHost, st), "rgb read");
+  }
+  if (tri_id) {
+    if (!c->last.ids) return fail(c, MR_E_INVALID, "ids were not requested for this frame");
+    CK(cudaMemcpyAsync(tri_id, c->last.ids, 4 * npx, cudaMemcpyDeviceToHost, st), "id read");
+  }
+  if (normals) {
+    if (!c->last.normals) return fail(c, MR_E_INVALID, "normals were not requested for this frame");
+    CK(cudaMemcpyAsync(normals, c->last.normals, 12 * npx, cudaMemcpyDeviceToHost, st), "normals read");
+  }
+  CK(cudaStreamSynchronize(st), "read wait");
+  return rc;
+}
+
+MR_API int mr_get_outputs(mr_ctx* c, mr_outputs* o) {
+  if (!c || !o) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  if (!c->have_frame) return fail(c, MR_E_INVALID, "no frame rendered yet");
+  o->width = c->last.W;
+  o->height = c->last.H;
+  o->rgb8 = c->last.rgb8;
+  o->depth = c->last.depth;
+  o->rgb_f32 = c->last.rgbf;
+  o->tri_id = c->last.ids;
+  o->normals = c->last.normals;
+  return MR_OK;
+}
+
+MR_API int mr_get_stats(mr_ctx* c, mr_stats* s) {
+  if (!c || !s) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  int rc = settle(c);
+  if (rc && rc != MR_E_BAD_INDEX) return rc;
+  memset(s, 0, sizeof(*s));
+  const Counters& k = *c->h_cnt;
+  s->triangles = c->last.n_tris;
+  s->clipped = (int64_t)k.clipped;
+  s->rasterised = (int64_t)k.rasterised;
+  s->small_direct = (int64_t)k.small_direct;
+  s->binned = (int64_t)k.rec_count;
+  s->bin_entries = (int64_t)k.bin_needed;
+  s->error_flags = k.error_flags;
+  if (c->profiling) {
+    s->n_stages = 5;
+    for (int i = 0; i < 5; i++) cudaEventElapsedTime(&s->stage_ms[i], c->ev[i], c->ev[i + 1]);
+  }
+  return rc;
+}
+
+MR_API int mr_read_range_image(mr_ctx* c, float* xyz) {
+  if (!c || !xyz) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  int rc = settle(c);
+  if (rc && rc != MR_E_BAD_INDEX) return rc;
+  if (!c->last.depth) return fail(c, MR_E_INVALID, "depth was not requested for this frame");
+  size_t npx = (size_t)c->last.W * c->last.H;
+  CK(c->range.ensure(3 * npx), "range buffer");
+  CK(launch_range(c->last.W, c->last.H, c->dP.p, c->last.depth, c->range.p, c->stream), "range launch");
+  CK(cudaMemcpyAsync(xyz, c->range.p, 12 * npx, cudaMemcpyDeviceToHost, c->stream), "range read");
+  CK(cudaStreamSynchronize(c->stream), "range wait");
+  return rc;
+}
+
+}  // extern "C"

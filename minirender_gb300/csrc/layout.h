@@ -1,0 +1,94 @@
+// Data layout shared by the host side of the C ABI and the kernels: one
+// resident mesh, one renderable of a frame, the setup record of a large
+// sub-triangle, per-frame counters and the kernel parameter block.  Plain
+// C++ (no device code), so host translation units can include it.
+#pragma once
+#include <stdint.h>
+
+#include "../../include/minirender_gpu.h"
+
+namespace mrg {
+
+// Packed visibility word: (order-preserving depth key << 32) | sub-triangle
+// id.  A pixel nobody wrote keeps VIS_EMPTY, which is larger than any real
+// fragment because real fragments need z < 1e11f (the clear value of the
+// reference z-buffer, src/Renderer.cpp:116) and id < 0xFFFFFFFF.
+static constexpr unsigned long long VIS_EMPTY = ~0ull;
+
+// One resident mesh (TriMesh arrays, include/minirender/Scene.h:73-87).
+struct DevMesh {
+  const float* pos;   // n_pos x 3
+  const float* nrm;   // n_nrm x 3
+  const float* uv;    // n_uv x 2
+  const int32_t* idx;   // 3 per triangle
+  const int32_t* nidx;
+  const int32_t* tidx;
+  const uint32_t* bad;   // bit t set: triangle t has an index out of range
+  int32_t n_pos, n_nrm, n_uv, n_tri;
+  int32_t has_uv;       // texcoords and texcoordsI both non-empty
+};
+
+// One renderable of the frame: mesh, matrices and material.
+struct DevRenderable {
+  float mv[12];         // rows 0..2 of view * transform (src/Renderer.cpp:337)
+  float nm[12];         // rows 0..2 of inverse(mv)^T (src/Renderer.cpp:338)
+  DevMesh mesh;
+  uint32_t tri_base;    // global index of the first triangle
+  int32_t has_tex;      // texturing on and the material has a texture
+  float diffuse[3], specular[3], emissive[3], shininess;
+  const uint8_t* tex8;  // rows x cols x 3 bytes (decoded b/255), or
+  const float* texf;    // rows x cols x 3 floats
+  int32_t tex_rows, tex_cols;
+};
+
+// Setup record of a sub-triangle too large for the setup kernel to
+// rasterise itself; 64 bytes, written once, read by the tile rasteriser.
+struct __align__(16) BigRec {
+  float p0x, p0y, p2x, p2y;   // pixel-space corners 0 and 2
+  float n1x, n1y, n2x, n2y;   // edge-function gradients
+  float z0, z1, z2;           // iz[] (perspective) or zz[] (orthographic)
+  uint32_t id;                // 2 * global triangle + clip sub-triangle
+  int32_t x0, y0, x1, y1;     // inclusive clamped pixel bounding box
+};
+
+struct Counters {
+  unsigned long long triangles, clipped, rasterised, small_direct, binned, bin_entries;
+  unsigned int error_flags;
+  unsigned int rec_count;      // big records written
+  unsigned int bin_needed;     // total (tile, record) pairs requested
+  unsigned int bin_overflow;
+};
+
+struct FrameParams {
+  int W, H;
+  float w, h;
+  float P[16];
+  int persp;
+  float znear;
+  float lightdir[3];
+  int point;
+  float ambient;
+  int lighting, save_normals;
+  float bg[3];
+  int n_renderables;
+  uint32_t n_tris;
+  int tile, tiles_x, tiles_y, small_max;
+  const DevRenderable* rs;
+  const uint32_t* tri_base;   // n_renderables + 1 prefix of triangle counts
+  unsigned long long* vis;    // W*H
+  BigRec* recs;
+  uint32_t rec_cap;
+  uint32_t* tile_count;       // tiles_x*tiles_y (+1 scanned into tile_start)
+  uint32_t* tile_start;
+  uint32_t* tile_fill;
+  uint32_t* bins;
+  uint32_t bin_cap;
+  uint8_t* rgb8;
+  float* depth;
+  float* rgbf;
+  uint32_t* ids;
+  float* normals;
+  Counters* counters;
+};
+
+}  // namespace mrg

@@ -1,0 +1,170 @@
+"""``Renderer``: the reference's public Renderer interface
+(include/minirender/Renderer.h:44-63) running on the GB300 path.
+
+Same method names and argument meaning as minirender::Renderer.  ``render``
+flattens the scene with Scene::collectShapes semantics, keeps meshes and
+textures resident on the device (re-uploaded only when a mesh's ``version``
+changes), and queues one frame through the C ABI; the getters read the
+results back.  The reference's paintMesh/paintTriangle are internal steps of
+``render`` here.
+"""
+from __future__ import annotations
+
+from typing import Dict, Optional
+
+import numpy as np
+
+from . import abi, capi
+from . import scene as sc
+from .frame import FrameState
+
+
+class Renderer:
+    def __init__(self, device: int = 0):
+        self.ctx = capi.Context(device)
+        self.state = FrameState()
+        self.scene: Optional[sc.SceneNode] = None
+        self._material = None
+        self._meshes: Dict[int, tuple] = {}     # id(TriMesh) -> (handle, version, mesh)
+        self._textures: Dict[int, tuple] = {}   # id(array) -> (handle, array)
+        self._out: Optional[dict] = None
+        self._rendered = False
+        self.outputs = abi.MR_OUT_DEFAULT | abi.MR_OUT_RGB_F32
+
+    # ---- setters, include/minirender/Renderer.h:45-55
+    def setSize(self, w: int, h: int):
+        self.state.width, self.state.height = int(w), int(h)
+        self.clear()
+
+    def aspect(self) -> float:
+        return float(np.float32(self.state.width) / np.float32(self.state.height))
+
+    def setScene(self, scene: sc.SceneNode):
+        self.scene = scene
+
+    def setProjection(self, m):
+        self.state.projection = np.asarray(m, np.float32).reshape(4, 4)
+
+    def setView(self, m):
+        self.state.view = np.asarray(m, np.float32).reshape(4, 4)
+
+    def setLight(self, v, point: bool = False):
+        self.state.light = np.asarray(v, np.float32).reshape(3)
+        self.state.light_is_point = bool(point)
+
+    def setMaterial(self, material: sc.Material):
+        # As in the reference, render() replaces the current material per mesh
+        # (src/Renderer.cpp:336), so this value is not used by render().
+        self._material = material
+
+    def setLighting(self, on: bool):
+        self.state.lighting = bool(on)
+
+    def setTexturing(self, on: bool):
+        self.state.texturing = bool(on)
+
+    def setSaveNormals(self, on: bool):
+        self.state.save_normals = bool(on)
+
+    def setBackground(self, color):
+        self.state.background = np.asarray(color, np.float32).reshape(3)
+
+    def clear(self):
+        """Renderer::clear (src/Renderer.cpp:113-119): background image,
+        depth 1e11f."""
+        self._out = None
+        self._rendered = False
+
+    # ---- frame
+    def _mesh_handle(self, mesh: sc.TriMesh) -> int:
+        rec = self._meshes.get(id(mesh))
+        if rec is not None and rec[2] is mesh:
+            h, ver, _ = rec
+            if ver != mesh.version:
+                self.ctx.update_mesh(h, mesh.desc())
+                self._meshes[id(mesh)] = (h, mesh.version, mesh)
+            return h
+        h = self.ctx.upload_mesh(mesh.desc())
+        self._meshes[id(mesh)] = (h, mesh.version, mesh)
+        return h
+
+    def _texture_handle(self, tex: np.ndarray) -> int:
+        rec = self._textures.get(id(tex))
+        if rec is not None and rec[1] is tex:
+            return rec[0]
+        h = self.ctx.upload_texture(tex)
+        self._textures[id(tex)] = (h, tex)
+        return h
+
+    def prepare(self):
+        """Flattens the scene (Scene::collectShapes), makes its meshes and
+        textures resident and returns the (mr_frame, renderables, count)
+        triple that mr_render takes."""
+        if self.scene is None:
+            raise RuntimeError("setScene() first")
+        flat = sc.flatten(self.scene)
+        rs, n = capi.collect_shapes(flat.nodes)
+        mesh_h = [self._mesh_handle(m) for m in flat.meshes]
+        tex_h = [self._texture_handle(t) for t in flat.textures]
+        for i in range(n):
+            rs[i].mesh = mesh_h[rs[i].mesh]
+            if rs[i].material.texture >= 0:
+                rs[i].material.texture = tex_h[rs[i].material.texture]
+        self.state.ambient = getattr(self.scene, "ambientLight", np.float32(0.1))
+        return self.state.to_c(), rs, n
+
+    def render(self):
+        """Renderer::render (src/Renderer.cpp:311-332)."""
+        frame, rs, n = self.prepare()
+        self.ctx.render(frame, rs, n, self.outputs)
+        self._out = None
+        self._rendered = True
+
+    def _read(self) -> dict:
+        if self._out is None:
+            if not self._rendered:
+                return self._cleared()
+            self._out = self.ctx.read(rgb8=True, depth=True, rgb_f32=True, tri_id=True,
+                                      normals=self.state.save_normals)
+        return self._out
+
+    def _cleared(self) -> dict:
+        H, W = self.state.height, self.state.width
+        img = np.empty((H, W, 3), np.float32)
+        img[:] = np.asarray(self.state.background, np.float32)
+        out = {"image": img, "depth": np.full((H, W), 1e11, np.float32),
+               "ids": np.full((H, W), abi.MR_NO_TRIANGLE, np.uint32)}
+        out["rgb8"] = np.clip(img * np.float32(255), 0, 255).astype(np.uint8)
+        if self.state.save_normals:
+            nrm = np.zeros((H, W, 3), np.float32)
+            nrm[..., 2] = 1
+            out["normals"] = nrm
+        return out
+
+    # ---- getters, include/minirender/Renderer.h:60-63
+    def getDepth(self) -> np.ndarray:
+        return self._read()["depth"]
+
+    def getImage(self) -> np.ndarray:
+        return self._read()["image"]
+
+    def getImageRGB8(self) -> np.ndarray:
+        """getImage() after savePPM's byte conversion (src/io.cpp:358-362)."""
+        return self._read()["rgb8"]
+
+    def getTriangleIds(self) -> np.ndarray:
+        """Visible sub-triangle per pixel: 2*(global triangle)+clip part."""
+        return self._read()["ids"]
+
+    def getRangeImage(self) -> np.ndarray:
+        self._read()
+        return self.ctx.range_image()
+
+    def getNormalsImage(self) -> np.ndarray:
+        return self._read()["normals"]
+
+    def stats(self) -> abi.mr_stats:
+        return self.ctx.stats()
+
+    def close(self):
+        self.ctx.close()

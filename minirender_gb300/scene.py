@@ -1,0 +1,158 @@
+"""Python mirror of minirender's scene model (include/minirender/Scene.h).
+
+Same class and member names as the reference so calling code reads the same:
+``Material`` (Scene.h:38-45, defaults src/Scene.cpp:65-71), ``SceneNode``
+(Scene.h:55-63), ``TriMesh`` (Scene.h:73-87) and ``Scene`` (Scene.h:89-95).
+Arrays are numpy: vertices/normals (N,3) float32, texcoords (N,2) float32,
+indices/normalsI/texcoordsI (3T,) int32, textures (rows, cols, 3) uint8
+(decoded as loadPPM does, src/io.cpp:407-410) or float32.
+
+``flatten`` turns a scene into the pre-order ``mr_node`` array that
+``mr_collect_shapes`` (the C restatement of Scene::collectShapes,
+src/Scene.cpp:13-36) consumes, plus the list of distinct meshes and
+textures it references.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional
+
+import numpy as np
+
+from . import abi
+
+
+def identity() -> np.ndarray:
+    return np.eye(4, dtype=np.float32)
+
+
+class Material:
+    """Material, include/minirender/Scene.h:38-45; defaults src/Scene.cpp:65-71."""
+
+    def __init__(self, diffuse=(0.7, 0.7, 0.9), specular=(0.8, 0.8, 0.8), emissive=(0, 0, 0),
+                 shininess=12.0, opacity=1.0, texture: Optional[np.ndarray] = None):
+        self.diffuse = np.asarray(diffuse, np.float32)
+        self.specular = np.asarray(specular, np.float32)
+        self.emissive = np.asarray(emissive, np.float32)
+        self.shininess = np.float32(shininess)
+        self.opacity = np.float32(opacity)
+        self.texture = texture  # (rows, cols, 3) uint8 or float32, or None
+
+
+class SceneNode:
+    """SceneNode, include/minirender/Scene.h:55-63."""
+
+    def __init__(self, transform: Optional[np.ndarray] = None):
+        self.visible = True
+        self.transform = identity() if transform is None else np.asarray(transform, np.float32)
+        self.children: List[SceneNode] = []
+
+    def add(self, node: "SceneNode") -> "SceneNode":
+        self.children.append(node)
+        return node
+
+
+class TriMesh(SceneNode):
+    """TriMesh, include/minirender/Scene.h:73-87."""
+
+    def __init__(self, vertices, normals, indices, normalsI=None, texcoords=None, texcoordsI=None,
+                 material: Optional[Material] = None, transform=None):
+        super().__init__(transform)
+        self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        self.normals = np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        self.indices = np.ascontiguousarray(indices, np.int32).reshape(-1)
+        self.normalsI = (self.indices if normalsI is None
+                         else np.ascontiguousarray(normalsI, np.int32).reshape(-1))
+        self.texcoords = (np.zeros((0, 2), np.float32) if texcoords is None
+                          else np.ascontiguousarray(texcoords, np.float32).reshape(-1, 2))
+        self.texcoordsI = (np.zeros(0, np.int32) if texcoordsI is None
+                           else np.ascontiguousarray(texcoordsI, np.int32).reshape(-1))
+        self.material = material
+        self.version = 0  # bump after editing arrays in place so resident copies refresh
+
+    @property
+    def n_triangles(self) -> int:
+        return self.indices.size // 3
+
+    def desc(self) -> abi.mr_mesh_desc:
+        """mr_mesh_desc pointing at this mesh's arrays (kept alive by self)."""
+        def p(a):
+            return a.ctypes.data if a.size else None
+        return abi.mr_mesh_desc(p(self.vertices), self.vertices.shape[0],
+                                p(self.normals), self.normals.shape[0],
+                                p(self.texcoords), self.texcoords.shape[0],
+                                p(self.indices), self.indices.size,
+                                p(self.normalsI), self.normalsI.size,
+                                p(self.texcoordsI), self.texcoordsI.size)
+
+
+class Scene(SceneNode):
+    """Scene, include/minirender/Scene.h:89-95 (ambientLight default 0.1)."""
+
+    def __init__(self):
+        super().__init__()
+        self.ambientLight = np.float32(0.1)
+        self.light = np.zeros(3, np.float32)
+
+
+def _fill_material(dst: abi.mr_material, m: Material, tex_index: int) -> None:
+    dst.diffuse[:] = [float(x) for x in m.diffuse]
+    dst.specular[:] = [float(x) for x in m.specular]
+    dst.emissive[:] = [float(x) for x in m.emissive]
+    dst.shininess = float(m.shininess)
+    dst.texture = tex_index
+
+
+class Flat:
+    """A scene flattened to the C-ABI's node form."""
+
+    def __init__(self, nodes, meshes: List[TriMesh], textures: List[np.ndarray]):
+        self.nodes = nodes
+        self.meshes = meshes
+        self.textures = textures
+
+
+def flatten(scene: SceneNode) -> Flat:
+    """Pre-order walk (parents before children, children in insertion order)."""
+    order = []
+    stack = [(scene, -1)]
+    while stack:
+        node, parent = stack.pop()
+        idx = len(order)
+        order.append((node, parent))
+        for ch in reversed(node.children):
+            stack.append((ch, idx))
+    nodes = (abi.mr_node * len(order))()
+    meshes: List[TriMesh] = []
+    mesh_ix = {}
+    textures: List[np.ndarray] = []
+    tex_ix = {}
+    for i, (node, parent) in enumerate(order):
+        nd = nodes[i]
+        nd.parent = parent
+        nd.transform[:] = [float(x) for x in np.asarray(node.transform, np.float32).reshape(16)]
+        nd.mesh = -1
+        nd.has_material = 0
+        if isinstance(node, TriMesh):
+            if id(node) not in mesh_ix:
+                mesh_ix[id(node)] = len(meshes)
+                meshes.append(node)
+            nd.mesh = mesh_ix[id(node)]
+            if node.material is not None:
+                t = -1
+                tex = node.material.texture
+                if tex is not None and tex.shape[0] > 0:
+                    if id(tex) not in tex_ix:
+                        tex_ix[id(tex)] = len(textures)
+                        textures.append(tex)
+                    t = tex_ix[id(tex)]
+                nd.has_material = 1
+                _fill_material(nd.material, node.material, t)
+    return Flat(nodes, meshes, textures)
+
+
+def mesh_descs(meshes: List[TriMesh]):
+    arr = (abi.mr_mesh_desc * max(1, len(meshes)))()
+    for i, m in enumerate(meshes):
+        arr[i] = m.desc()
+    return arr

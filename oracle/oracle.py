@@ -1,0 +1,256 @@
+"""ORACLE -- test infrastructure only: ctypes wrappers around
+
+* ``_build/libmr_oracle.so``: the C restatement in mr_oracle.c, and
+* ``_ref/libmr_ref.so``: the reference's own Renderer/Scene/primitives
+  compiled against the ASL stand-in (present only where the reference
+  sources were available at build time).
+
+Only tests, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this module; the product path never imports it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+from minirender_gb300 import abi
+from minirender_gb300 import scene as sc
+from minirender_gb300.frame import FrameState
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", "libmr_oracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libmr_ref.so")
+REF_SRC = "/root/reference"
+
+_lib = None
+_ref = None
+
+
+class _Tex(C.Structure):
+    _fields_ = [("rgb", C.c_void_p), ("rows", C.c_int32), ("cols", C.c_int32)]
+
+
+def build(with_ref: bool = True) -> None:
+    """Compile the restatement (always) and the reference build (when the
+    reference sources are present)."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if with_ref and os.path.isdir(os.path.join(REF_SRC, "src")):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_SRC], check=True)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_SO):
+            build(with_ref=False)
+        L = C.CDLL(ORACLE_SO)
+        L.mro_collect_shapes.restype = C.c_int
+        L.mro_collect_shapes.argtypes = [C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                         C.POINTER(C.c_int32)]
+        L.mro_render.restype = C.c_int
+        L.mro_render.argtypes = [C.POINTER(abi.mr_frame), C.c_void_p, C.c_int32, C.c_void_p,
+                                 C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p]
+        L.mro_quantize_rgb8.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
+        L.mro_decode_rgb8.argtypes = [C.c_void_p, C.c_int64, C.c_void_p]
+        L.mro_range_image.argtypes = [C.POINTER(abi.mr_frame), C.c_void_p, C.c_void_p]
+        for n in ("mro_mat4_mul",):
+            getattr(L, n).argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.mro_mat4_inverse.argtypes = [C.c_void_p, C.c_void_p]
+        L.mro_projection_frustum.argtypes = [C.c_float] * 4 + [C.c_void_p]
+        L.mro_render_frames_mt.restype = C.c_double
+        L.mro_render_frames_mt.argtypes = [C.POINTER(abi.mr_frame), C.c_void_p, C.c_int32,
+                                           C.c_void_p, C.c_int32, C.c_void_p, C.c_int32,
+                                           C.c_int32, C.c_int32]
+        _lib = L
+    return _lib
+
+
+def ref_lib() -> Optional[C.CDLL]:
+    """The reference build, or None where it cannot exist."""
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_SO):
+            if not os.path.isdir(os.path.join(REF_SRC, "src")):
+                return None
+            build(with_ref=True)
+        L = C.CDLL(REF_SO)
+        L.ref_render.restype = C.c_int
+        L.ref_render.argtypes = [C.POINTER(abi.mr_frame), C.c_void_p, C.c_int32, C.c_void_p,
+                                 C.c_int32, C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.c_void_p]
+        L.ref_primitive.restype = C.c_int
+        L.ref_primitive.argtypes = [C.c_int, C.c_float, C.c_float, C.c_int, C.c_int, C.c_int,
+                                    C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]
+        L.ref_projection.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
+        L.ref_mat4_mul.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_mat4_inverse.argtypes = [C.c_void_p, C.c_void_p]
+        _ref = L
+    return _ref
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data
+
+
+def decode_rgb8(tex: np.ndarray) -> np.ndarray:
+    """loadPPM texel decode (src/io.cpp:407-410) via the C restatement."""
+    tex = np.ascontiguousarray(tex, np.uint8)
+    out = np.empty(tex.shape, np.float32)
+    lib().mro_decode_rgb8(_ptr(tex), tex.size // 3, _ptr(out))
+    return out
+
+
+def quantize_rgb8(image: np.ndarray) -> np.ndarray:
+    """savePPM conversion (src/io.cpp:358-362) via the C restatement."""
+    image = np.ascontiguousarray(image, np.float32)
+    out = np.empty(image.shape, np.uint8)
+    lib().mro_quantize_rgb8(_ptr(image), image.size // 3, _ptr(out))
+    return out
+
+
+def _float_textures(textures):
+    keep = []
+    arr = (_Tex * max(1, len(textures)))()
+    for i, t in enumerate(textures):
+        f = decode_rgb8(t) if t.dtype == np.uint8 else np.ascontiguousarray(t, np.float32)
+        keep.append(f)
+        arr[i].rgb = _ptr(f)
+        arr[i].rows = f.shape[0]
+        arr[i].cols = f.shape[1]
+    return arr, keep
+
+
+def collect_shapes(flat: sc.Flat):
+    n_nodes = len(flat.nodes)
+    out = (abi.mr_renderable * max(1, n_nodes))()
+    n = C.c_int32(0)
+    rc = lib().mro_collect_shapes(C.addressof(flat.nodes), n_nodes, C.addressof(out), n_nodes,
+                                  C.byref(n))
+    if rc != 0:
+        raise RuntimeError(f"mro_collect_shapes failed: {rc}")
+    return out, n.value
+
+
+def render(state: FrameState, scene: sc.SceneNode, normals: bool = False) -> dict:
+    """The C restatement: image (H,W,3) f32, depth (H,W) f32, ids (H,W) u32,
+    rgb8 (H,W,3) u8 and optionally normals."""
+    flat = sc.flatten(scene)
+    rs, n = collect_shapes(flat)
+    meshes = sc.mesh_descs(flat.meshes)
+    tex, keep = _float_textures(flat.textures)
+    f = state.to_c()
+    H, W = state.height, state.width
+    image = np.empty((H, W, 3), np.float32)
+    depth = np.empty((H, W), np.float32)
+    ids = np.empty((H, W), np.uint32)
+    nrm = np.empty((H, W, 3), np.float32) if normals else None
+    rc = lib().mro_render(C.byref(f), C.addressof(rs), n, C.addressof(meshes), len(flat.meshes),
+                          C.addressof(tex), len(flat.textures), _ptr(image), _ptr(depth), _ptr(ids),
+                          _ptr(nrm) if nrm is not None else None)
+    if rc != 0:
+        raise RuntimeError(f"mro_render failed: {rc}")
+    out = {"image": image, "depth": depth, "ids": ids, "rgb8": quantize_rgb8(image)}
+    if nrm is not None:
+        out["normals"] = nrm
+    return out
+
+
+def range_image(state: FrameState, depth: np.ndarray) -> np.ndarray:
+    f = state.to_c()
+    depth = np.ascontiguousarray(depth, np.float32)
+    out = np.empty(depth.shape + (3,), np.float32)
+    lib().mro_range_image(C.byref(f), _ptr(depth), _ptr(out))
+    return out
+
+
+def time_frames(state: FrameState, scene: sc.SceneNode, n_frames: int, n_threads: int) -> float:
+    """Seconds for n_frames independent renders on n_threads host threads."""
+    flat = sc.flatten(scene)
+    rs, n = collect_shapes(flat)
+    meshes = sc.mesh_descs(flat.meshes)
+    tex, keep = _float_textures(flat.textures)
+    f = state.to_c()
+    return lib().mro_render_frames_mt(C.byref(f), C.addressof(rs), n, C.addressof(meshes),
+                                      len(flat.meshes), C.addressof(tex), len(flat.textures),
+                                      n_frames, n_threads)
+
+
+def ref_render(state: FrameState, scene: sc.SceneNode, normals: bool = False,
+               range_xyz: bool = False) -> dict:
+    """The reference Renderer itself (compiled from its sources)."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference build unavailable")
+    flat = sc.flatten(scene)
+    meshes = sc.mesh_descs(flat.meshes)
+    tex, keep = _float_textures(flat.textures)
+    f = state.to_c()
+    H, W = state.height, state.width
+    image = np.empty((H, W, 3), np.float32)
+    depth = np.empty((H, W), np.float32)
+    nrm = np.empty((H, W, 3), np.float32) if normals else None
+    rng = np.empty((H, W, 3), np.float32) if range_xyz else None
+    rc = L.ref_render(C.byref(f), C.addressof(flat.nodes), len(flat.nodes), C.addressof(meshes),
+                      len(flat.meshes), C.addressof(tex), len(flat.textures), _ptr(image),
+                      _ptr(depth), _ptr(nrm) if nrm is not None else None,
+                      _ptr(rng) if rng is not None else None)
+    if rc != 0:
+        raise RuntimeError(f"ref_render failed: {rc}")
+    out = {"image": image, "depth": depth, "rgb8": quantize_rgb8(image)}
+    if nrm is not None:
+        out["normals"] = nrm
+    if rng is not None:
+        out["range"] = rng
+    return out
+
+
+def ref_primitive(kind: int, a: float, b: float = 0.0, seg: int = 0, hseg: int = 0,
+                  caps: bool = True) -> dict:
+    """Arrays from the reference's createCube(0)/createCylinder(1)/createSphere(2)."""
+    L = ref_lib()
+    counts = np.zeros(5, np.int32)
+    L.ref_primitive(kind, a, b, seg, hseg, int(caps), _ptr(counts), None, None, None, None, None)
+    v = np.empty((counts[0], 3), np.float32)
+    n = np.empty((counts[1], 3), np.float32)
+    t = np.empty((counts[2], 2), np.float32)
+    i = np.empty(counts[3], np.int32)
+    ni = np.empty(counts[4], np.int32)
+    L.ref_primitive(kind, a, b, seg, hseg, int(caps), _ptr(counts), _ptr(v), _ptr(n), _ptr(t),
+                    _ptr(i), _ptr(ni))
+    return {"vertices": v, "normals": n, "texcoords": t, "indices": i, "normalsI": ni}
+
+
+def ref_projection(kind: int, params) -> np.ndarray:
+    p = np.asarray(params, np.float32)
+    out = np.empty(16, np.float32)
+    ref_lib().ref_projection(kind, _ptr(p), _ptr(out))
+    return out.reshape(4, 4)
+
+
+def ref_mat4_mul(a, b) -> np.ndarray:
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    out = np.empty(16, np.float32)
+    ref_lib().ref_mat4_mul(_ptr(a), _ptr(b), _ptr(out))
+    return out.reshape(4, 4)
+
+
+def mat4_mul(a, b) -> np.ndarray:
+    a = np.ascontiguousarray(a, np.float32)
+    b = np.ascontiguousarray(b, np.float32)
+    out = np.empty(16, np.float32)
+    lib().mro_mat4_mul(_ptr(a), _ptr(b), _ptr(out))
+    return out.reshape(4, 4)
+
+
+def mat4_inverse(a) -> np.ndarray:
+    a = np.ascontiguousarray(a, np.float32)
+    out = np.empty(16, np.float32)
+    lib().mro_mat4_inverse(_ptr(a), _ptr(out))
+    return out.reshape(4, 4)

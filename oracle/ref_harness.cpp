@@ -1,0 +1,182 @@
+// ORACLE -- test infrastructure only.  C entry points that drive the
+// reference's own minirender::Renderer (src/Renderer.cpp), Scene
+// (src/Scene.cpp) and primitive generators (src/primitives.cpp), compiled
+// unmodified against the ASL stand-in in oracle/asl_shim by oracle/Makefile.
+// The product never loads this; tests use it to pin mr_oracle.c.
+#include <string.h>
+
+#include <vector>
+
+#include "minirender/Renderer.h"
+#include "minirender/primitives.h"
+#include "../include/minirender_gpu.h"
+
+using namespace asl;
+using namespace minirender;
+
+static Matrix4 to_m4(const float* m) {
+  return Matrix4(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], m[11], m[12],
+                 m[13], m[14], m[15]);
+}
+static void from_m4(const Matrix4& a, float* m) {
+  for (int i = 0; i < 4; i++)
+    for (int j = 0; j < 4; j++) m[4 * i + j] = a(i, j);
+}
+
+struct RefTexture {
+  const float* rgb;
+  int32_t rows, cols;
+};
+
+static Shared<TriMesh> make_mesh(const mr_mesh_desc& d) {
+  Shared<TriMesh> m = new TriMesh();
+  for (int i = 0; i < d.n_vertices; i++)
+    m->vertices << Vec3(d.vertices[3 * i], d.vertices[3 * i + 1], d.vertices[3 * i + 2]);
+  for (int i = 0; i < d.n_normals; i++)
+    m->normals << Vec3(d.normals[3 * i], d.normals[3 * i + 1], d.normals[3 * i + 2]);
+  for (int i = 0; i < d.n_texcoords; i++) m->texcoords << Vec2(d.texcoords[2 * i], d.texcoords[2 * i + 1]);
+  for (int i = 0; i < d.n_indices; i++) m->indices << d.indices[i];
+  for (int i = 0; i < d.n_normalsI; i++) m->normalsI << d.normalsI[i];
+  for (int i = 0; i < d.n_texcoordsI; i++) m->texcoordsI << d.texcoordsI[i];
+  return m;
+}
+
+extern "C" {
+
+// Builds a Scene from a pre-order node array (node 0 = the Scene root) and
+// renders it with the reference Renderer.  normals may be NULL.
+int ref_render(const mr_frame* f, const mr_node* nodes, int32_t n_nodes, const mr_mesh_desc* meshes,
+               int32_t n_meshes, const RefTexture* tex, int32_t n_tex, float* image, float* depth,
+               float* normals, float* range_xyz) {
+  if (n_nodes < 1 || nodes[0].parent != -1 || nodes[0].mesh != -1) return MR_E_INVALID;
+  Shared<Scene> scene = new Scene();
+  scene->transform = to_m4(nodes[0].transform);
+  scene->ambientLight = f->ambient;
+  std::vector<Shared<SceneNode>> made(n_nodes);
+  made[0] = scene;
+  for (int i = 1; i < n_nodes; i++) {
+    const mr_node& nd = nodes[i];
+    if (nd.parent < 0 || nd.parent >= i) return MR_E_INVALID;
+    Shared<SceneNode> node;
+    if (nd.mesh >= 0) {
+      if (nd.mesh >= n_meshes) return MR_E_HANDLE;
+      Shared<TriMesh> m = make_mesh(meshes[nd.mesh]);
+      if (nd.has_material) {
+        Shared<Material> mat = new Material();
+        mat->diffuse = Vec3(nd.material.diffuse[0], nd.material.diffuse[1], nd.material.diffuse[2]);
+        mat->specular = Vec3(nd.material.specular[0], nd.material.specular[1], nd.material.specular[2]);
+        mat->emissive = Vec3(nd.material.emissive[0], nd.material.emissive[1], nd.material.emissive[2]);
+        mat->shininess = nd.material.shininess;
+        int t = nd.material.texture;
+        if (t >= 0) {
+          if (t >= n_tex) return MR_E_HANDLE;
+          mat->texture.resize(tex[t].rows, tex[t].cols);
+          for (int a = 0; a < tex[t].rows; a++)
+            for (int b = 0; b < tex[t].cols; b++) {
+              const float* p = tex[t].rgb + 3 * ((size_t)a * tex[t].cols + b);
+              mat->texture(a, b) = Vec3(p[0], p[1], p[2]);
+            }
+        }
+        m->material = mat;
+      }
+      node = m;
+    } else {
+      node = new SceneNode();
+    }
+    node->transform = to_m4(nd.transform);
+    made[nd.parent]->children << node;
+    made[i] = node;
+  }
+  Renderer r;
+  r.setSaveNormals(f->save_normals != 0);
+  r.setBackground(Vec3(f->background[0], f->background[1], f->background[2]));
+  r.setSize(f->width, f->height);
+  r.setScene(scene);
+  r.setProjection(to_m4(f->projection));
+  r.setView(to_m4(f->view));
+  r.setLight(Vec3(f->light[0], f->light[1], f->light[2]), f->light_is_point != 0);
+  r.setLighting(f->lighting != 0);
+  r.setTexturing(f->texturing != 0);
+  r.render();
+  Array2<Vec3> img = r.getImage();
+  Array2<float> dep = r.getDepth();
+  size_t npx = (size_t)f->width * f->height;
+  for (size_t i = 0; i < npx; i++) {
+    const Vec3& v = img.data()[i];
+    image[3 * i] = v.x;
+    image[3 * i + 1] = v.y;
+    image[3 * i + 2] = v.z;
+    depth[i] = dep.data()[i];
+  }
+  if (normals && f->save_normals) {
+    Array2<Vec3> nrm = r.getNormalsImage();
+    for (size_t i = 0; i < npx; i++) {
+      normals[3 * i] = nrm.data()[i].x;
+      normals[3 * i + 1] = nrm.data()[i].y;
+      normals[3 * i + 2] = nrm.data()[i].z;
+    }
+  }
+  if (range_xyz) {
+    Array2<Vec3> pts = r.getRangeImage();
+    for (size_t i = 0; i < npx; i++) {
+      range_xyz[3 * i] = pts.data()[i].x;
+      range_xyz[3 * i + 1] = pts.data()[i].y;
+      range_xyz[3 * i + 2] = pts.data()[i].z;
+    }
+  }
+  return MR_OK;
+}
+
+// Reference primitive generators.  kind: 0 cube(a), 1 cylinder(a, b, seg,
+// hseg, caps), 2 sphere(a, lat=seg, lon=hseg).  Call with NULL buffers to get
+// the counts (vertices, normals, texcoords, indices).
+int ref_primitive(int kind, float a, float b, int seg, int hseg, int caps, int32_t* counts,
+                  float* vertices, float* normals, float* texcoords, int32_t* indices,
+                  int32_t* normalsI) {
+  Shared<TriMesh> m;
+  if (kind == 0) m = createCube(a);
+  else if (kind == 1) m = createCylinder(a, b, seg, hseg, caps != 0);
+  else if (kind == 2) m = createSphere(a, seg, hseg);
+  else return MR_E_INVALID;
+  counts[0] = m->vertices.length();
+  counts[1] = m->normals.length();
+  counts[2] = m->texcoords.length();
+  counts[3] = m->indices.length();
+  counts[4] = m->normalsI.length();
+  if (vertices)
+    for (int i = 0; i < counts[0]; i++) {
+      vertices[3 * i] = m->vertices[i].x; vertices[3 * i + 1] = m->vertices[i].y; vertices[3 * i + 2] = m->vertices[i].z;
+    }
+  if (normals)
+    for (int i = 0; i < counts[1]; i++) {
+      normals[3 * i] = m->normals[i].x; normals[3 * i + 1] = m->normals[i].y; normals[3 * i + 2] = m->normals[i].z;
+    }
+  if (texcoords)
+    for (int i = 0; i < counts[2]; i++) {
+      texcoords[2 * i] = m->texcoords[i].x; texcoords[2 * i + 1] = m->texcoords[i].y;
+    }
+  if (indices) memcpy(indices, m->indices.ptr(), sizeof(int32_t) * counts[3]);
+  if (normalsI) memcpy(normalsI, m->normalsI.ptr(), sizeof(int32_t) * counts[4]);
+  return MR_OK;
+}
+
+// Reference projection builders (src/Renderer.cpp:40-83).  kind: 0 ortho,
+// 1 perspective (l,r,b,t,n,f); 2 frustum, 3 frustumH, 4 ortho-fov (fov,
+// aspect, n, f in p[0..3]).
+void ref_projection(int kind, const float* p, float* out) {
+  Matrix4 m;
+  switch (kind) {
+    case 0: m = projectionOrtho(p[0], p[1], p[2], p[3], p[4], p[5]); break;
+    case 1: m = projectionPerspective(p[0], p[1], p[2], p[3], p[4], p[5]); break;
+    case 2: m = projectionFrustum(p[0], p[1], p[2], p[3]); break;
+    case 3: m = projectionFrustumH(p[0], p[1], p[2], p[3]); break;
+    default: m = projectionOrtho(p[0], p[1], p[2], p[3]); break;
+  }
+  from_m4(m, out);
+}
+
+// Matrix4 product / inverse as the stand-in ASL computes them.
+void ref_mat4_mul(const float* a, const float* b, float* out) { from_m4(to_m4(a) * to_m4(b), out); }
+void ref_mat4_inverse(const float* a, float* out) { from_m4(to_m4(a).inverse(), out); }
+
+}  // extern "C"

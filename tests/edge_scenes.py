@@ -1,0 +1,170 @@
+"""Hand-built scenes for the edge cases of the reference rasteriser
+(src/Renderer.cpp:121-309): exact depth ties, shared edges, the three
+clipTriangle cases and its |dz| < 1e-6 branch, degenerate and off-screen
+triangles, texture wrap-around, orthographic depth below zero, large
+triangles spanning many tiles, lighting variants."""
+import numpy as np
+
+from minirender_gb300 import projection as pj
+from minirender_gb300.frame import FrameState
+from minirender_gb300.scene import Material, Scene, TriMesh
+
+f32 = np.float32
+
+
+def _tri_mesh(verts, tris, normals=None, uvs=None, material=None):
+    verts = np.asarray(verts, np.float32).reshape(-1, 3)
+    tris = np.asarray(tris, np.int32).reshape(-1)
+    if normals is None:
+        normals = np.tile(np.array([[0, 0, 1]], np.float32), (verts.shape[0], 1))
+    kw = {}
+    if uvs is not None:
+        kw = dict(texcoords=np.asarray(uvs, np.float32), texcoordsI=tris)
+    return TriMesh(verts, normals, tris, normalsI=tris, material=material, **kw)
+
+
+def _persp(w, h, near=0.5, far=100.0, fov=60):
+    return pj.projection_frustum(pj.deg2rad(fov), f32(w) / f32(h), near, far)
+
+
+def ties(w=96, h=64):
+    """Two coplanar copies of a quad with different colours in one mesh and a
+    third copy in a later renderable: the first drawn must win every tie."""
+    v = [[-1, -1, -3], [1, -1, -3], [1, 1, -3], [-1, 1, -3]]
+    quad = [0, 1, 2, 0, 2, 3]
+    sc = Scene()
+    m1 = _tri_mesh(v, quad + quad, material=Material(diffuse=(1, 0, 0)))
+    m2 = _tri_mesh(v, quad, material=Material(diffuse=(0, 0, 1)))
+    sc.add(m1)
+    sc.add(m2)
+    st = FrameState(width=w, height=h, projection=_persp(w, h), light=np.array([0, 0, 1], np.float32))
+    return st, sc
+
+
+def shared_edges(w=97, h=71):
+    """A fan of thin triangles sharing edges and a vertex at a pixel centre."""
+    n = 24
+    ang = np.linspace(0, 2 * np.pi, n, endpoint=False)
+    v = [[0, 0, -4]] + [[1.7 * np.cos(a), 1.7 * np.sin(a), -4] for a in ang]
+    tris = []
+    for i in range(n):
+        tris += [0, 1 + i, 1 + (i + 1) % n]
+    sc = Scene()
+    sc.add(_tri_mesh(v, tris, material=Material(diffuse=(0.2, 0.9, 0.4), shininess=0)))
+    st = FrameState(width=w, height=h, projection=_persp(w, h), light=np.array([0.3, 0.2, 1], np.float32))
+    return st, sc
+
+
+def near_clip(w=128, h=96):
+    """Triangles crossing the near plane (z = -0.5) in all three
+    configurations, in every vertex rotation, plus one whose crossing edge
+    has |dz| < 1e-6 (clip() then uses k = 0.5)."""
+    zn = -0.5
+    tris_v = []
+    for rot in range(3):
+        for pattern in ([1, 1, 0], [1, 0, 1], [0, 1, 1], [1, 0, 0], [0, 1, 0], [0, 0, 1]):
+            pts = []
+            for c, inside in enumerate(pattern):
+                ang = 2 * np.pi * c / 3 + rot * 0.7
+                z = zn + 0.3 if inside else zn - 1.5 - 0.2 * c
+                pts.append([0.8 * np.cos(ang) + 0.9 * (rot - 1), 0.8 * np.sin(ang), z])
+            tris_v.append(pts)
+    # |dz| < 1e-6 across the plane
+    tris_v.append([[-0.2, -0.6, zn + 4e-7], [0.2, -0.6, zn - 4e-7], [0.0, -0.2, zn - 2.0]])
+    verts = np.array(tris_v, np.float32).reshape(-1, 3)
+    tris = np.arange(verts.shape[0], dtype=np.int32)
+    # keep only front-facing windings so something is drawn; flip the others
+    t = tris.reshape(-1, 3).copy()
+    sc = Scene()
+    both = np.concatenate([t, t[:, [0, 2, 1]]]).reshape(-1)
+    uvs = np.random.default_rng(5).uniform(0, 1, (verts.shape[0], 2)).astype(np.float32)
+    tex = np.random.default_rng(6).integers(0, 256, (16, 16, 3)).astype(np.uint8)
+    nrm = np.random.default_rng(7).normal(size=(verts.shape[0], 3)).astype(np.float32)
+    m = TriMesh(verts, nrm, both, normalsI=both, texcoords=uvs, texcoordsI=both,
+                material=Material(texture=tex, shininess=20))
+    sc.add(m)
+    st = FrameState(width=w, height=h, projection=_persp(w, h, near=0.5, fov=90),
+                    light=np.array([0.2, 0.5, 1], np.float32), light_is_point=True)
+    return st, sc
+
+
+def degenerate_offscreen(w=80, h=60):
+    """Collinear (a == 0) and zero-area triangles, triangles entirely and
+    partly off screen, one covering the whole screen."""
+    v = [[0, 0, -3], [1, 1, -3], [2, 2, -3],            # collinear
+         [0.5, 0.5, -3], [0.5, 0.5, -3], [0.6, 0.4, -3],  # repeated vertex
+         [40, 40, -3], [41, 40, -3], [40, 41, -3],       # off screen
+         [-2.5, -0.3, -2], [-0.9, -0.5, -2], [-2.0, 0.9, -2],  # partly off screen (left)
+         [-30, -30, -9], [30, -30, -9], [0, 40, -9]]     # full screen, far
+    tris = list(range(15))
+    sc = Scene()
+    sc.add(_tri_mesh(v, tris, material=Material(diffuse=(0.9, 0.8, 0.1), emissive=(0.05, 0, 0))))
+    st = FrameState(width=w, height=h, projection=_persp(w, h),
+                    background=np.array([0.1, 0.2, 0.3], np.float32))
+    return st, sc
+
+
+def texture_wrap(w=64, h=64):
+    """UVs well outside [0,1]: fract() wraps the texel lookup; float texture."""
+    v = [[-1, -1, -2.5], [1, -1, -2.5], [1, 1, -2.5], [-1, 1, -2.5]]
+    uvs = [[0.25, 0.25], [3.75, 0.25], [3.75, 2.6], [0.25, 2.6]]
+    tex = np.random.default_rng(11).uniform(0, 1, (7, 5, 3)).astype(np.float32)
+    sc = Scene()
+    sc.add(_tri_mesh(v, [0, 1, 2, 0, 2, 3], uvs=uvs, material=Material(texture=tex, shininess=0)))
+    st = FrameState(width=w, height=h, projection=_persp(w, h))
+    return st, sc
+
+
+def ortho_negative_z(w=90, h=70):
+    """Orthographic projection (P(3,3) = 1): depth is NDC z, part of it < 0,
+    two interpenetrating triangles, lighting off (emissive only)."""
+    v = [[-3, -2, -60], [3, -2, -90], [0, 3, -70],
+         [-3, 2, -95], [3, 2, -55], [0, -3, -75]]
+    sc = Scene()
+    sc.add(_tri_mesh(v, [0, 1, 2], material=Material(emissive=(0.9, 0.1, 0.2))))
+    sc.add(_tri_mesh(v, [3, 5, 4], material=Material(emissive=(0.1, 0.9, 0.2))))
+    st = FrameState(width=w, height=h, projection=pj.projection_ortho(-4, 4, -3, 3, 50, 120),
+                    lighting=False)
+    return st, sc
+
+
+def big_triangles(w=300, h=200):
+    """Large overlapping triangles spanning many screen tiles (binned path),
+    interleaved with tiny ones (direct path)."""
+    rng = np.random.default_rng(21)
+    verts, tris = [], []
+    for k in range(12):
+        c = rng.uniform(-1.5, 1.5, 2)
+        r = rng.uniform(0.8, 3.0)
+        z = -rng.uniform(2.5, 6.0)
+        a0 = rng.uniform(0, 2 * np.pi)
+        base = len(verts)
+        for j in range(3):
+            a = a0 - 2 * np.pi * j / 3
+            verts.append([c[0] + r * np.cos(a), c[1] + r * np.sin(a), z + rng.uniform(-0.5, 0.5)])
+        tris += [base, base + 2, base + 1]
+        for _ in range(20):
+            p = rng.uniform(-2, 2, 2)
+            zz = -rng.uniform(2.5, 6.0)
+            base = len(verts)
+            s = 0.02
+            verts += [[p[0], p[1], zz], [p[0], p[1] + s, zz], [p[0] + s, p[1], zz]]
+            tris += [base, base + 2, base + 1]
+    nrm = rng.normal(size=(len(verts), 3)).astype(np.float32)
+    sc = Scene()
+    sc.add(TriMesh(np.array(verts, np.float32), nrm, np.array(tris, np.int32),
+                   material=Material(diffuse=(0.6, 0.6, 0.7), shininess=40)))
+    st = FrameState(width=w, height=h, projection=_persp(w, h, near=1.0),
+                    light=np.array([1, 2, 2], np.float32), light_is_point=True, save_normals=True)
+    return st, sc
+
+
+ALL = {
+    "ties": ties,
+    "shared_edges": shared_edges,
+    "near_clip": near_clip,
+    "degenerate_offscreen": degenerate_offscreen,
+    "texture_wrap": texture_wrap,
+    "ortho_negative_z": ortho_negative_z,
+    "big_triangles": big_triangles,
+}

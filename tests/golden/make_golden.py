@@ -1,0 +1,46 @@
+#!/usr/bin/env python3
+"""Regenerates tests/golden/*.npz: small seeded scenes rendered by the
+reference's own Renderer (src/Renderer.cpp, src/Scene.cpp compiled unmodified
+against the ASL stand-in by oracle/Makefile).  Needs the reference sources;
+run from the repository root:  python tests/golden/make_golden.py
+Each fixture stores its inputs, so the check does not depend on the
+platform's math library regenerating identical scenes."""
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+import edge_scenes as E  # noqa: E402
+from golden_io import save_case  # noqa: E402
+from minirender_gb300 import workloads as W  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+
+def cases():
+    yield "config1_128x96", W.config1(128, 96)
+    yield "config2_l4_128x72", W.config2(level=4, width=128, height=72, tex_size=32)
+    yield "config3_4k_128x72", W.config3(n_tris=4000, width=128, height=72)
+    st, sc = W.config4_scene(3, n_prims=10, resolution=(128, 96))
+    yield "config4_s3_128x96", (st, sc)
+    for name, fn in sorted(E.ALL.items()):
+        yield "edge_" + name, fn(128, 96) if name == "big_triangles" else fn()
+
+
+def main():
+    if O.ref_lib() is None:
+        sys.exit("reference sources not available")
+    for name, (st, sc) in cases():
+        r = O.ref_render(st, sc, normals=st.save_normals)
+        expect = {"image": r["image"], "depth": r["depth"]}
+        if st.save_normals:
+            expect["normals"] = r["normals"]
+        path = os.path.join(HERE, name + ".npz")
+        save_case(path, st, sc, expect)
+        print(f"{name}: {os.path.getsize(path) / 1024:.0f} KiB")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,122 @@
+"""CPU tests of the oracle: the C restatement against the reference's own
+sources (compiled against the ASL stand-in) where they are present, and
+against the committed golden fixtures everywhere."""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import edge_scenes as E
+from minirender_gb300 import projection as pj
+from minirender_gb300 import workloads as W
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def _bits_equal(a, b):
+    return np.array_equal(np.ascontiguousarray(a).view(np.uint32), np.ascontiguousarray(b).view(np.uint32))
+
+
+def _vs_ref(st, sc, normals=False):
+    o = O.render(st, sc, normals=normals)
+    r = O.ref_render(st, sc, normals=normals)
+    assert _bits_equal(o["image"], r["image"]), "image differs from the reference build"
+    assert _bits_equal(o["depth"], r["depth"]), "depth differs from the reference build"
+    if normals:
+        assert _bits_equal(o["normals"], r["normals"])
+    return o
+
+
+def test_config1_vs_reference(oracle_lib, ref_lib):
+    st, sc = W.config1()
+    o = _vs_ref(st, sc)
+    assert (o["ids"] != 0xFFFFFFFF).sum() > 50_000
+
+
+def test_config2_reduced_vs_reference(oracle_lib, ref_lib):
+    st, sc = W.config2(level=6, width=480, height=270, tex_size=256)
+    o = _vs_ref(st, sc)
+    assert ((o["ids"] & 1) == 1).sum() > 0  # second half of a clipped quad wins pixels
+
+
+def test_config3_reduced_vs_reference(oracle_lib, ref_lib):
+    st, sc = W.config3(n_tris=100_000, width=640, height=360)
+    _vs_ref(st, sc)
+
+
+@pytest.mark.parametrize("seed", [0, 5])
+def test_config4_vs_reference(oracle_lib, ref_lib, seed):
+    st, sc = W.config4_scene(seed)
+    _vs_ref(st, sc)
+
+
+@pytest.mark.parametrize("name", sorted(E.ALL))
+def test_edge_vs_reference(oracle_lib, ref_lib, name):
+    st, sc = E.ALL[name]()
+    _vs_ref(st, sc, normals=st.save_normals)
+
+
+def test_range_image_vs_reference(oracle_lib, ref_lib):
+    st, sc = W.config1(160, 120)
+    o = O.render(st, sc)
+    r = O.ref_render(st, sc, range_xyz=True)
+    assert _bits_equal(O.range_image(st, o["depth"]), r["range"])
+
+
+def test_primitives_vs_reference(ref_lib):
+    """The numpy primitive generators produce the reference's topology and
+    its positions within one float32 rounding (trig in double, rounded)."""
+    cases = [(W.create_cube(1.0), (0, 1.0, 0, 0, 0)), (W.create_sphere(1.0, 32, 64), (2, 1.0, 0, 32, 64)),
+             (W.create_cylinder(0.5, 1.2, 17), (1, 0.5, 1.2, 17, 1))]
+    for mesh, (kind, a, b, seg, hseg) in cases:
+        ref = O.ref_primitive(kind, a, b, seg, hseg)
+        assert np.array_equal(mesh.indices, ref["indices"])
+        assert np.array_equal(mesh.normalsI, ref["normalsI"])
+        for k in ("vertices", "normals", "texcoords"):
+            x, y = getattr(mesh, k), ref[k]
+            assert x.shape == y.shape
+            assert np.allclose(x, y, rtol=0, atol=1e-6), k
+
+
+def test_projection_builders_vs_reference(ref_lib):
+    np.testing.assert_array_equal(pj.projection_ortho(-40, 40, -30, 30, 50, 120),
+                                  O.ref_projection(0, [-40, 40, -30, 30, 50, 120]))
+    np.testing.assert_array_equal(pj.projection_perspective(-1, 1.5, -0.7, 0.9, 0.3, 50),
+                                  O.ref_projection(1, [-1, 1.5, -0.7, 0.9, 0.3, 50]))
+    a = pj.projection_frustum(pj.deg2rad(45), np.float32(640) / np.float32(480), 0.1, 100)
+    b = O.ref_projection(2, [pj.deg2rad(45), np.float32(640) / np.float32(480), 0.1, 100])
+    np.testing.assert_allclose(a, b, rtol=2e-7)
+
+
+def test_mat4_ops_vs_reference(ref_lib):
+    rng = np.random.default_rng(0)
+    for _ in range(200):
+        a = rng.normal(size=(4, 4)).astype(np.float32)
+        b = rng.normal(size=(4, 4)).astype(np.float32)
+        assert _bits_equal(O.mat4_mul(a, b), O.ref_mat4_mul(a, b))
+        assert _bits_equal(pj.mat_mul(a, b), O.ref_mat4_mul(a, b))
+
+
+# ---------------------------------------------------------------- golden fixtures
+def _load_fixture(path):
+    from golden_io import load_case
+    return load_case(path)
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "*.npz"))),
+                         ids=lambda p: os.path.basename(p)[:-4])
+def test_oracle_matches_golden(oracle_lib, path):
+    """Outputs of the reference's own Renderer, recorded by
+    tests/golden/make_golden.py, reproduced bit for bit by the oracle."""
+    st, sc, expect = _load_fixture(path)
+    o = O.render(st, sc, normals=st.save_normals)
+    assert _bits_equal(o["image"], expect["image"])
+    assert _bits_equal(o["depth"], expect["depth"])
+    if "normals" in expect:
+        assert _bits_equal(o["normals"], expect["normals"])
+
+
+def test_golden_fixtures_present():
+    assert len(glob.glob(os.path.join(GOLDEN, "*.npz"))) >= 8

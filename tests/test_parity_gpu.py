@@ -1,0 +1,88 @@
+"""Device path vs the oracle on the benchmark configurations and edge cases
+(bit-exact ids and depth, RGB8 within 1 LSB on >= 99.9% of pixels)."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import edge_scenes as E
+from parity import assert_parity, compare, gpu_render
+from minirender_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REPORT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
+
+
+def _report(stats):
+    os.makedirs(REPORT, exist_ok=True)
+    with open(os.path.join(REPORT, "parity.jsonl"), "a") as f:
+        f.write(json.dumps(stats) + "\n")
+
+
+@pytest.fixture(scope="module")
+def renderer(product_lib):
+    from minirender_gb300.renderer import Renderer
+    r = Renderer(0)
+    yield r
+    r.close()
+
+
+def _check(name, st, sc, renderer, **kw):
+    ref = O.render(st, sc, normals=st.save_normals)
+    gpu, _ = gpu_render(st, sc, renderer, **kw)
+    stats = compare(gpu, ref, name)
+    if st.save_normals:
+        stats["normals_max_err"] = float(np.abs(gpu["normals"] - ref["normals"]).max())
+    _report(stats)
+    assert_parity(stats)
+    return stats
+
+
+def test_config1(renderer):
+    st, sc = W.config1()
+    _check("config1", st, sc, renderer)
+
+
+def test_config2_full(renderer):
+    st, sc = W.config2()
+    s = _check("config2", st, sc, renderer)
+    assert s["covered"] > 500_000
+
+
+def test_config3_scaled(renderer):
+    st, sc = W.config3(n_tris=1_000_000, width=1920, height=1080)
+    _check("config3_1M_1080p", st, sc, renderer)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_config4_scenes(renderer, seed):
+    st, sc = W.config4_scene(seed)
+    _check(f"config4_{seed}", st, sc, renderer)
+
+
+@pytest.mark.parametrize("name", sorted(E.ALL))
+def test_edge(renderer, name):
+    st, sc = E.ALL[name]()
+    _check(name, st, sc, renderer)
+
+
+@pytest.mark.parametrize("tile,small", [(8, 0), (16, 4096), (32, 16), (16, 1)])
+def test_tuning_variants_same_result(renderer, tile, small):
+    """Tile size and the small-triangle limit change the work split, never
+    the result."""
+    st, sc = W.config2(level=6, width=640, height=360, tex_size=256)
+    try:
+        _check(f"tuning_{tile}_{small}", st, sc, renderer, tile=tile, small_max=small)
+    finally:
+        renderer.ctx.set_tuning(16, 64)
+
+
+def test_deterministic(renderer):
+    st, sc = W.config4_scene(7)
+    a, _ = gpu_render(st, sc, renderer)
+    b, _ = gpu_render(st, sc, renderer)
+    for k in ("ids", "depth", "rgb8", "image"):
+        assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
