@@ -47,6 +47,7 @@ extern "C" {
 #define MR_E_TIMEOUT -7      /* a bounded device wait gave up */
 #define MR_E_NOT_READY -8    /* asynchronous result not available yet */
 #define MR_E_NO_DEVICE -9    /* no usable CUDA device */
+#define MR_E_NOALLOC_LIMIT -10 /* frame or mesh larger than mr_render_noalloc's fixed scratch */
 
 /* Background sentinel in the per-pixel triangle-id image. */
 #define MR_NO_TRIANGLE 0xFFFFFFFFu
@@ -196,6 +197,42 @@ MR_API int mr_get_stats(mr_ctx* ctx, mr_stats* out);
 /* Replaces: Renderer::getRangeImage (src/Renderer.cpp:388-415): view-space
  * XYZ per pixel from the last depth buffer, H*W*3 floats to host memory. */
 MR_API int mr_read_range_image(mr_ctx* ctx, float* xyz);
+
+/* ---- rendering without any device allocation ----------------------------
+ * No counterpart in the reference (its CPU Renderer never touches device
+ * memory).  For callers that must not allocate device memory themselves or
+ * through this library: code running under a framework whose pool owns all
+ * device memory, or a real-time loop that cannot afford cudaMalloc/cudaFree
+ * and the device-wide synchronisation cudaFree implies.  Renders one mesh
+ * (one renderable of Renderer::render, src/Renderer.cpp:311-381) with every
+ * piece of working memory -- visibility buffer, counters, tile table,
+ * per-triangle index-check mask, renderable record -- taken from one
+ * file-scope device array of MR_NOALLOC_SCRATCH_BYTES that the library
+ * reserves on each GPU it is loaded on, until the process exits.
+ *
+ * Limits: width, height <= MR_NOALLOC_MAX_SIDE, width*height <=
+ * MR_NOALLOC_MAX_PIXELS, triangles <= MR_NOALLOC_MAX_TRIANGLES; anything
+ * larger returns MR_E_NOALLOC_LIMIT before any device work.
+ * Inputs and outputs are DEVICE pointers owned by the caller: the mesh arrays
+ * in *mesh (same layout as mr_mesh_upload's), the texture (rows x cols x 3
+ * bytes decoded as b/255, or floats; NULL for none), and the outputs rgb8
+ * (H*W*3), depth (H*W), tri_id (H*W), any of which may be NULL.  Results are
+ * bit-identical to mr_render of the same renderable.
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call
+ * before any stream capture.  The call is synchronous on `cuda_stream`
+ * (NULL = legacy default stream).  All calls in the process share the one
+ * scratch array, which keeps the previous call's contents: calls whose GPU
+ * work overlaps (other host threads, other streams) race on it and must be
+ * serialised by the caller. */
+#define MR_NOALLOC_SCRATCH_BYTES (17u << 20)
+#define MR_NOALLOC_MAX_SIDE 4096
+#define MR_NOALLOC_MAX_PIXELS (1 << 21)
+#define MR_NOALLOC_MAX_TRIANGLES (1 << 22)
+MR_API int mr_render_noalloc(const mr_frame* frame, const mr_mesh_desc* mesh, const float* transform,
+                             const mr_material* material, const void* texture, int32_t tex_rows,
+                             int32_t tex_cols, int32_t tex_is_rgb8, uint8_t* rgb8, float* depth,
+                             uint32_t* tri_id, void* cuda_stream);
 
 /* ---- host helpers (no device work) -------------------------------------- */
 /* Scene::collectShapes (src/Scene.cpp:13-36) over a pre-order node array.

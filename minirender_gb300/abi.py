@@ -15,6 +15,10 @@ MR_E_BUDGET = -6
 MR_E_TIMEOUT = -7
 MR_E_NOT_READY = -8
 MR_E_NO_DEVICE = -9
+MR_E_NOALLOC_LIMIT = -10
+MR_NOALLOC_MAX_SIDE = 4096
+MR_NOALLOC_MAX_PIXELS = 1 << 21
+MR_NOALLOC_MAX_TRIANGLES = 1 << 22
 MR_NO_TRIANGLE = 0xFFFFFFFF
 
 MR_OUT_RGB8 = 1

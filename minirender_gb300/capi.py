@@ -42,6 +42,8 @@ _SIGS = {
     "mr_get_outputs": ([_P, C.POINTER(abi.mr_outputs)], C.c_int),
     "mr_get_stats": ([_P, C.POINTER(abi.mr_stats)], C.c_int),
     "mr_read_range_image": ([_P, _P], C.c_int),
+    "mr_render_noalloc": ([C.POINTER(abi.mr_frame), C.POINTER(abi.mr_mesh_desc), _P,
+                           C.POINTER(abi.mr_material), _P, _I, _I, _I, _P, _P, _P, _P], C.c_int),
     "mr_collect_shapes": ([_P, _I, _P, _I, C.POINTER(_I)], C.c_int),
     "mr_mat4_mul": ([_P, _P, _P], None),
     "mr_mat4_inverse": ([_P, _P], None),

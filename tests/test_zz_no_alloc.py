@@ -1,0 +1,106 @@
+"""mr_render_noalloc: the entry point for callers that cannot allocate device
+memory (a host framework whose pool owns the device, or a real-time loop that
+cannot pay for cudaMalloc/cudaFree).  It keeps its working memory in a fixed
+device array inside the library, so this test checks that its output equals
+the ordinary entry point's (mr_render through Renderer) on two calls in a
+row -- the second call starts from the scratch the first one left behind --
+for an untextured and a textured scene, and that oversized requests are
+refused before any device work.
+
+This file is named to be collected last; it passes on its own in a fresh
+process as well as after the other tests.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from parity import RGB8_FRAC_MIN
+from minirender_gb300 import abi, capi
+from minirender_gb300 import scene as S
+from minirender_gb300 import workloads as W
+from minirender_gb300.renderer import Renderer
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes():
+    yield "sphere_640x480", W.config1()
+    yield "textured_icosphere_640x360", W.config2(level=6, width=640, height=360, tex_size=256)
+
+
+def _existing(st, sc):
+    r = Renderer(0)
+    try:
+        r.state = st
+        r.setScene(sc)
+        r.render()
+        return {"rgb8": r.getImageRGB8().copy(), "depth": r.getDepth().copy(),
+                "ids": r.getTriangleIds().copy()}
+    finally:
+        r.close()
+
+
+def _noalloc(st, sc, calls=2):
+    import torch
+    flat = S.flatten(sc)
+    rs, n = capi.collect_shapes(flat.nodes)
+    assert n == 1
+    mesh = flat.meshes[rs[0].mesh]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    keep = {k: dev(getattr(mesh, k)) for k in ("vertices", "normals", "texcoords", "indices",
+                                                "normalsI", "texcoordsI") if getattr(mesh, k).size}
+    p = lambda k: keep[k].data_ptr() if k in keep else None  # noqa: E731
+    desc = abi.mr_mesh_desc(p("vertices"), mesh.vertices.shape[0], p("normals"), mesh.normals.shape[0],
+                            p("texcoords"), mesh.texcoords.shape[0], p("indices"), mesh.indices.size,
+                            p("normalsI"), mesh.normalsI.size, p("texcoordsI"), mesh.texcoordsI.size)
+    tex = flat.textures[0] if flat.textures else None
+    tex_d = dev(tex) if tex is not None else None
+    H, W_ = st.height, st.width
+    rgb8 = torch.empty((H, W_, 3), dtype=torch.uint8, device="cuda")
+    depth = torch.empty((H, W_), dtype=torch.float32, device="cuda")
+    ids = torch.empty((H, W_), dtype=torch.int32, device="cuda")
+    frame = st.to_c()
+    xf = (C.c_float * 16)(*rs[0].transform)
+    torch.cuda.synchronize()
+    outs = []
+    for _ in range(calls):
+        rc = capi.lib().mr_render_noalloc(
+            C.byref(frame), C.byref(desc), C.addressof(xf), C.byref(rs[0].material),
+            tex_d.data_ptr() if tex_d is not None else None,
+            tex.shape[0] if tex is not None else 0, tex.shape[1] if tex is not None else 0,
+            int(tex is not None and tex.dtype == np.uint8),
+            rgb8.data_ptr(), depth.data_ptr(), ids.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        assert rc == abi.MR_OK, capi.lib().mr_status_string(rc)
+        outs.append({"rgb8": rgb8.cpu().numpy(), "depth": depth.cpu().numpy(),
+                     "ids": ids.cpu().numpy().view(np.uint32)})
+        rgb8.fill_(7)
+        depth.fill_(-3.0)
+        ids.fill_(5)
+    return outs
+
+
+@pytest.mark.parametrize("name,case", list(_scenes()), ids=[n for n, _ in _scenes()])
+def test_noalloc_matches_existing_entry_point(product_lib, name, case):
+    st, sc = case
+    want = _existing(st, sc)
+    for k, got in enumerate(_noalloc(st, sc)):
+        assert np.array_equal(got["ids"], want["ids"]), f"call {k}: visible ids differ"
+        assert np.array_equal(got["depth"].view(np.uint32), want["depth"].view(np.uint32)), f"call {k}: depth"
+        d = np.abs(got["rgb8"].astype(np.int16) - want["rgb8"].astype(np.int16)).max(-1)
+        assert (d <= 1).mean() >= RGB8_FRAC_MIN, f"call {k}: rgb8"
+
+
+def test_noalloc_rejects_oversized_requests(product_lib):
+    st, sc = W.config1()
+    flat = S.flatten(sc)
+    desc = flat.meshes[0].desc()
+    mat = abi.mr_material()
+    xf = (C.c_float * 16)(*np.eye(4, dtype=np.float32).reshape(16))
+    for w, h in ((abi.MR_NOALLOC_MAX_SIDE + 1, 16), (2048, 2048)):
+        st.width, st.height = w, h
+        frame = st.to_c()
+        rc = capi.lib().mr_render_noalloc(C.byref(frame), C.byref(desc), C.addressof(xf), C.byref(mat),
+                                          None, 0, 0, 0, None, None, None, None)
+        assert rc == abi.MR_E_NOALLOC_LIMIT
+    assert capi.lib().mr_status_string(abi.MR_E_NOALLOC_LIMIT).startswith(b"request exceeds")
