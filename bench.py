@@ -189,8 +189,8 @@ def cpu_frames_per_s(st, sc, n_threads: int, frames: int):
     return frames / secs, secs
 
 
-STAGES = ["clear", "setup", "bin", "tile_raster", "resolve"]
-KERNELS = {"clear": "k_clear", "setup": "k_setup", "bin": "k_bin_count+k_scan+k_bin_scatter",
+STAGES = ["clear+vertex", "setup", "bin", "tile_raster", "resolve"]
+KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "bin": "k_bin_count+k_scan+k_bin_scatter",
            "tile_raster": "k_tile_raster", "resolve": "k_resolve"}
 
 
@@ -306,7 +306,7 @@ def gpu_arm(args, ws, rank, local):
     tex_px = P if flat.textures else 0
     n_big = int(stats.binned)
     alg = {
-        "clear": 8 * P,
+        "clear+vertex": 8 * P + 12 * V + 24 * V + 16 * V,
         "setup": 12 * T + 12 * V + 64 * n_big,
         "bin": 2 * 64 * n_big + 8 * int(stats.bin_entries),
         "tile_raster": 64 * int(stats.bin_entries),

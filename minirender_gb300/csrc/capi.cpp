@@ -84,7 +84,9 @@ struct mr_ctx {
   DevBuf<uint32_t> bins;
   DevBuf<uint32_t> tiles;
   DevBuf<DevRenderable> rs;
-  DevBuf<uint32_t> tri_base;
+  DevBuf<uint32_t> tri_base;   // tri, vertex and normal base tables, 3 x (n+1)
+  DevBuf<float4> va, vn;        // per-frame vertex-pass outputs
+  DevBuf<float2> vb;
   DevBuf<float> dP;
   DevRenderable* h_rs = nullptr;
   size_t h_rs_cap = 0;
@@ -184,6 +186,7 @@ MR_API int mr_destroy(mr_ctx* c) {
     c->vis.release(); c->rgb8.release(); c->depth.release(); c->rgbf.release();
     c->normals.release(); c->range.release(); c->ids.release(); c->recs.release();
     c->bins.release(); c->tiles.release(); c->rs.release(); c->tri_base.release(); c->dP.release();
+    c->va.release(); c->vb.release(); c->vn.release();
     if (c->h_rs) cudaFreeHost(c->h_rs);
     if (c->h_tri_base) cudaFreeHost(c->h_tri_base);
     if (c->d_cnt) cudaFree(c->d_cnt);
@@ -439,12 +442,15 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     c->h_tri_base = nullptr;
     c->h_rs_cap = 0;
     CK(cudaMallocHost(&c->h_rs, sizeof(DevRenderable) * nrs), "pinned staging");
-    CK(cudaMallocHost(&c->h_tri_base, sizeof(uint32_t) * (nrs + 1)), "pinned staging");
+    CK(cudaMallocHost(&c->h_tri_base, sizeof(uint32_t) * 3 * (nrs + 1)), "pinned staging");
     c->h_rs_cap = nrs;
   } else {
     CK(cudaEventSynchronize(c->staged), "staging wait");
   }
   uint32_t base = 0;
+  uint64_t vbase = 0, nbase = 0;
+  uint32_t* h_vbase = c->h_tri_base + (n + 1);
+  uint32_t* h_nbase = c->h_tri_base + 2 * (n + 1);
   for (int32_t i = 0; i < n; i++) {
     const MeshRec& m = c->meshes[rs[i].mesh];
     DevRenderable& R = c->h_rs[i];
@@ -458,6 +464,14 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     R.tri_base = base;
     c->h_tri_base[i] = base;
     base += (uint32_t)m.d.n_tri;
+    R.vert_base = (uint32_t)vbase;
+    R.nrm_base = (uint32_t)nbase;
+    h_vbase[i] = (uint32_t)vbase;
+    h_nbase[i] = (uint32_t)nbase;
+    vbase += (uint64_t)m.d.n_pos;
+    nbase += (uint64_t)m.d.n_nrm;
+    if (vbase >= ((uint64_t)1 << 32) || nbase >= ((uint64_t)1 << 32))
+      return fail(c, MR_E_INVALID, "more than 2^32-1 vertices or normals in one frame");
     const mr_material& M = rs[i].material;
     memcpy(R.diffuse, M.diffuse, sizeof(R.diffuse));
     memcpy(R.specular, M.specular, sizeof(R.specular));
@@ -477,6 +491,8 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     }
   }
   c->h_tri_base[n] = base;
+  h_vbase[n] = (uint32_t)vbase;
+  h_nbase[n] = (uint32_t)nbase;
 
   const int W = f->width, H = f->height;
   const size_t npx = (size_t)W * H;
@@ -492,9 +508,12 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   CK(c->tiles.ensure((size_t)3 * tx * ty + 1), "tile buffer");
   if (c->bins.cap < ((size_t)1 << 20)) CK(c->bins.ensure((size_t)1 << 20), "bin buffer");
   CK(c->rs.ensure(nrs), "renderable table");
-  CK(c->tri_base.ensure(nrs + 1), "triangle base table");
+  CK(c->tri_base.ensure(3 * (nrs + 1)), "base tables");
+  CK(c->va.ensure(vbase), "vertex buffer");
+  CK(c->vb.ensure(vbase), "vertex buffer");
+  CK(c->vn.ensure(nbase), "normal buffer");
   CK(cudaMemcpyAsync(c->rs.p, c->h_rs, sizeof(DevRenderable) * n, cudaMemcpyHostToDevice, c->stream), "renderable upload");
-  CK(cudaMemcpyAsync(c->tri_base.p, c->h_tri_base, sizeof(uint32_t) * (n + 1), cudaMemcpyHostToDevice, c->stream), "base upload");
+  CK(cudaMemcpyAsync(c->tri_base.p, c->h_tri_base, sizeof(uint32_t) * 3 * (n + 1), cudaMemcpyHostToDevice, c->stream), "base upload");
   CK(cudaMemcpyAsync(c->dP.p, f->projection, sizeof(float) * 16, cudaMemcpyHostToDevice, c->stream), "projection upload");
   CK(cudaEventRecord(c->staged, c->stream), "staging event");
 
@@ -524,6 +543,13 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   F.small_max = c->small_max;
   F.rs = c->rs.p;
   F.tri_base = c->tri_base.p;
+  F.vert_base = c->tri_base.p + (n + 1);
+  F.nrm_base = c->tri_base.p + 2 * (n + 1);
+  F.n_verts = (uint32_t)vbase;
+  F.n_nrms = (uint32_t)nbase;
+  F.va = c->va.p;
+  F.vb = c->vb.p;
+  F.vn = c->vn.p;
   F.vis = c->vis.p;
   F.recs = c->recs.p;
   F.rec_cap = (uint32_t)std::min<size_t>(c->recs.cap, 0xFFFFFFFFu);

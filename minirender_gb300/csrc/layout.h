@@ -4,6 +4,7 @@
 // C++ (no device code), so host translation units can include it.
 #pragma once
 #include <stdint.h>
+#include <vector_types.h>
 
 #include "../../include/minirender_gpu.h"
 
@@ -34,6 +35,8 @@ struct DevRenderable {
   float nm[12];         // rows 0..2 of inverse(mv)^T (src/Renderer.cpp:338)
   DevMesh mesh;
   uint32_t tri_base;    // global index of the first triangle
+  uint32_t vert_base;   // global index of the first vertex in the per-frame vertex buffers
+  uint32_t nrm_base;    // global index of the first normal
   int32_t has_tex;      // texturing on and the material has a texture
   float diffuse[3], specular[3], emissive[3], shininess;
   const uint8_t* tex8;  // rows x cols x 3 bytes (decoded b/255), or
@@ -75,6 +78,14 @@ struct FrameParams {
   int tile, tiles_x, tiles_y, small_max;
   const DevRenderable* rs;
   const uint32_t* tri_base;   // n_renderables + 1 prefix of triangle counts
+  const uint32_t* vert_base;  // n_renderables + 1 prefix of vertex counts
+  const uint32_t* nrm_base;   // n_renderables + 1 prefix of normal counts
+  uint32_t n_verts, n_nrms;
+  // Per-frame vertex buffers written by the vertex pass (null: the setup and
+  // resolve kernels transform vertices themselves, per triangle).
+  float4* va;                 // (pixel x, pixel y, z term, view z) per vertex
+  float2* vb;                 // (view x, view y) per vertex
+  float4* vn;                 // view-space normal per normal
   unsigned long long* vis;    // W*H
   BigRec* recs;
   uint32_t rec_cap;

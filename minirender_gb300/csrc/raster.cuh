@@ -27,6 +27,11 @@ __device__ __forceinline__ float minr(float a, float b) { return (b < a) ? b : a
 __device__ __forceinline__ float maxr(float a, float b) { return (a < b) ? b : a; }
 __device__ __forceinline__ float clampr(float x, float lo, float hi) { return (x < lo) ? lo : ((x > hi) ? hi : x); }
 
+// 1/x correctly rounded (IEEE round-to-nearest reciprocal): the same value
+// as the division 1.0f/x, at the cost of a reciprocal.  Also -1/x == -(1/x)
+// exactly, since IEEE division rounds the magnitude independently of signs.
+__device__ __forceinline__ float rcp(float x) { return __frcp_rn(x); }
+
 // Matrix4 * Vec3 with the affine rows of a row-major matrix.
 __device__ __forceinline__ V3 affine(const float* m, V3 p) {
   return v3(m[0] * p.x + m[1] * p.y + m[2] * p.z + m[3],
