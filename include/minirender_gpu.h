@@ -198,6 +198,35 @@ MR_API int mr_get_stats(mr_ctx* ctx, mr_stats* out);
  * XYZ per pixel from the last depth buffer, H*W*3 floats to host memory. */
 MR_API int mr_read_range_image(mr_ctx* ctx, float* xyz);
 
+/* ---- batches -------------------------------------------------------------
+ * No single counterpart in the reference: many Renderer::render() calls
+ * (src/Renderer.cpp:311-332), one per scene, done in one launch sequence --
+ * vertex pass, setup of every scene's triangles into records binned per
+ * screen tile, and one persistent fused bin-raster-shade kernel over the
+ * tiles of all scenes.  Results per scene are identical to mr_render's. */
+typedef struct mr_batch_scene {
+    mr_frame frame;                 /* the scene's Renderer state */
+    int32_t first_renderable;       /* its renderables: renderables[first .. first+n) */
+    int32_t n_renderables;
+} mr_batch_scene;
+
+/* Tile edge (8/16/32), threads per tile block (64/128/256) and records
+ * staged per pass in shared memory (16..256) for mr_render_batch. */
+MR_API int mr_set_batch_tuning(mr_ctx* ctx, int tile, int threads, int chunk);
+/* graphs != 0: the launch sequence is captured once per batch shape (scene
+ * count, sizes, renderable and triangle counts, tuning) into a CUDA graph and
+ * replayed; cameras, lights and materials may change between replays. */
+MR_API int mr_set_batch_graphs(mr_ctx* ctx, int graphs);
+/* Queues the batch; outputs: MR_OUT_RGB8 | MR_OUT_DEPTH | MR_OUT_TRI_ID. */
+MR_API int mr_render_batch(mr_ctx* ctx, const mr_batch_scene* scenes, int32_t n_scenes,
+                           const mr_renderable* renderables, int32_t n_renderables, int32_t outputs);
+/* Waits for the last batch and copies scene `scene`'s outputs to host memory. */
+MR_API int mr_read_batch(mr_ctx* ctx, int32_t scene, uint8_t* rgb8, float* depth, uint32_t* tri_id);
+/* Device pointers of scene `scene`'s outputs (valid until the next batch). */
+MR_API int mr_get_batch_outputs(mr_ctx* ctx, int32_t scene, mr_outputs* out);
+/* Waits for the last batch; counters and stage times (vertex, setup, fused). */
+MR_API int mr_get_batch_stats(mr_ctx* ctx, mr_stats* out);
+
 /* ---- rendering without any device allocation ----------------------------
  * No counterpart in the reference (its CPU Renderer never touches device
  * memory).  For callers that must not allocate device memory themselves or

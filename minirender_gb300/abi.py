@@ -74,3 +74,7 @@ class mr_stats(C.Structure):
     _fields_ = [("triangles", C.c_int64), ("clipped", C.c_int64), ("rasterised", C.c_int64),
                 ("small_direct", C.c_int64), ("binned", C.c_int64), ("bin_entries", C.c_int64),
                 ("error_flags", C.c_int64), ("stage_ms", C.c_float * 8), ("n_stages", C.c_int32)]
+
+
+class mr_batch_scene(C.Structure):
+    _fields_ = [("frame", mr_frame), ("first_renderable", C.c_int32), ("n_renderables", C.c_int32)]

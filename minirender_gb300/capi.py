@@ -44,6 +44,12 @@ _SIGS = {
     "mr_read_range_image": ([_P, _P], C.c_int),
     "mr_render_noalloc": ([C.POINTER(abi.mr_frame), C.POINTER(abi.mr_mesh_desc), _P,
                            C.POINTER(abi.mr_material), _P, _I, _I, _I, _P, _P, _P, _P], C.c_int),
+    "mr_set_batch_tuning": ([_P, C.c_int, C.c_int, C.c_int], C.c_int),
+    "mr_set_batch_graphs": ([_P, C.c_int], C.c_int),
+    "mr_render_batch": ([_P, _P, _I, _P, _I, _I], C.c_int),
+    "mr_read_batch": ([_P, _I, _P, _P, _P], C.c_int),
+    "mr_get_batch_outputs": ([_P, _I, C.POINTER(abi.mr_outputs)], C.c_int),
+    "mr_get_batch_stats": ([_P, C.POINTER(abi.mr_stats)], C.c_int),
     "mr_collect_shapes": ([_P, _I, _P, _I, C.POINTER(_I)], C.c_int),
     "mr_mat4_mul": ([_P, _P, _P], None),
     "mr_mat4_inverse": ([_P, _P], None),
@@ -195,6 +201,40 @@ class Context:
         rc = lib().mr_get_stats(self.h, C.byref(s))
         if rc not in (0, abi.MR_E_BAD_INDEX):
             self._check(rc, "mr_get_stats")
+        return s
+
+    # ---- batches
+    def set_batch_tuning(self, tile: int, threads: int, chunk: int):
+        self._check(lib().mr_set_batch_tuning(self.h, tile, threads, chunk), "mr_set_batch_tuning")
+
+    def set_batch_graphs(self, on: bool):
+        self._check(lib().mr_set_batch_graphs(self.h, int(on)), "mr_set_batch_graphs")
+
+    def render_batch(self, scenes, n_scenes: int, renderables, n_rs: int,
+                     outputs: int = abi.MR_OUT_DEFAULT):
+        self._batch_hw = [(scenes[i].frame.height, scenes[i].frame.width) for i in range(n_scenes)]
+        self._check(lib().mr_render_batch(self.h, C.addressof(scenes), n_scenes,
+                                          C.addressof(renderables) if n_rs else None, n_rs, outputs),
+                    "mr_render_batch")
+
+    def read_batch(self, scene: int, rgb8=True, depth=True, tri_id=True) -> dict:
+        H, W = self._batch_hw[scene]
+        out = {}
+        if rgb8:
+            out["rgb8"] = np.empty((H, W, 3), np.uint8)
+        if depth:
+            out["depth"] = np.empty((H, W), np.float32)
+        if tri_id:
+            out["ids"] = np.empty((H, W), np.uint32)
+        self._check(lib().mr_read_batch(self.h, scene, _ptr(out.get("rgb8")), _ptr(out.get("depth")),
+                                        _ptr(out.get("ids"))), "mr_read_batch")
+        return out
+
+    def batch_stats(self) -> abi.mr_stats:
+        s = abi.mr_stats()
+        rc = lib().mr_get_batch_stats(self.h, C.byref(s))
+        if rc not in (0, abi.MR_E_BAD_INDEX):
+            self._check(rc, "mr_get_batch_stats")
         return s
 
     def outputs(self) -> abi.mr_outputs:

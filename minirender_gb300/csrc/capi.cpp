@@ -24,6 +24,9 @@ cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st);
 cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev);
 cudaError_t launch_range(int W, int H, const float* dP, const float* depth, float* xyz,
                          cudaStream_t st);
+cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
+                         cudaEvent_t* ev);
+int batch_grid(int tile, int chunk, int threads);
 }  // namespace mrg
 
 using namespace mrg;
@@ -104,6 +107,41 @@ struct mr_ctx {
   mr_frame last_frame{};
   int outputs = 0;
   std::string err;
+
+  // ---- batches
+  struct Batch {
+    int tile = 16, threads = 256, chunk = 64;
+    bool graphs = true;
+    DevBuf<DevRenderable> rs;
+    DevBuf<uint32_t> bases;
+    DevBuf<SceneRec> scenes;
+    DevBuf<uint32_t> stb;
+    DevBuf<float4> va, vn;
+    DevBuf<float2> vb;
+    DevBuf<BigRec> recs;
+    DevBuf<uint32_t> rec_scene, tiles, bins, block_sums;
+    DevBuf<uint8_t> out8;
+    DevBuf<float> outd;
+    DevBuf<uint32_t> outi;
+    DevRenderable* h_rs = nullptr;
+    size_t h_rs_cap = 0;
+    uint32_t* h_u32 = nullptr;  // bases (3(n+1)) then scene tile bases (S+1)
+    size_t h_u32_cap = 0;
+    SceneRec* h_scenes = nullptr;
+    size_t h_scenes_cap = 0;
+    Counters* d_cnt = nullptr;
+    Counters* h_cnt = nullptr;
+    BatchParams P{};
+    int grid = 0;
+    int n_scenes = 0, n_rs = 0;
+    std::vector<int> W, H;
+    std::vector<size_t> px_off;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    std::vector<uint64_t> key;
+    cudaEvent_t done = nullptr;
+    bool have = false;
+  } b;
 };
 
 static int fail(mr_ctx* c, int code, const std::string& msg) {
@@ -164,6 +202,9 @@ MR_API int mr_create(int device, mr_ctx** out) {
   for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming);
   if (e == cudaSuccess) e = c->dP.ensure(16);
+  if (e == cudaSuccess) e = cudaMalloc(&c->b.d_cnt, sizeof(Counters));
+  if (e == cudaSuccess) e = cudaMallocHost(&c->b.h_cnt, sizeof(Counters));
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->b.done, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     delete c;
     return e == cudaErrorMemoryAllocation ? MR_E_NOMEM : MR_E_CUDA;
@@ -194,6 +235,18 @@ MR_API int mr_destroy(mr_ctx* c) {
     for (auto& e : c->ev)
       if (e) cudaEventDestroy(e);
     if (c->staged) cudaEventDestroy(c->staged);
+    auto& B = c->b;
+    B.rs.release(); B.bases.release(); B.scenes.release(); B.stb.release(); B.va.release(); B.vn.release();
+    B.vb.release(); B.recs.release(); B.rec_scene.release(); B.tiles.release(); B.bins.release();
+    B.block_sums.release(); B.out8.release(); B.outd.release(); B.outi.release();
+    if (B.h_rs) cudaFreeHost(B.h_rs);
+    if (B.h_u32) cudaFreeHost(B.h_u32);
+    if (B.h_scenes) cudaFreeHost(B.h_scenes);
+    if (B.d_cnt) cudaFree(B.d_cnt);
+    if (B.h_cnt) cudaFreeHost(B.h_cnt);
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    if (B.graph) cudaGraphDestroy(B.graph);
+    if (B.done) cudaEventDestroy(B.done);
     if (c->own) cudaStreamDestroy(c->own);
   }
   delete c;
@@ -519,37 +572,37 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
 
   FrameParams& F = c->last;
   memset(&F, 0, sizeof(F));
-  F.W = W;
-  F.H = H;
-  F.w = (float)W;
-  F.h = (float)H;
-  memcpy(F.P, f->projection, sizeof(F.P));
+  F.v.W = W;
+  F.v.H = H;
+  F.v.w = (float)W;
+  F.v.h = (float)H;
+  memcpy(F.v.P, f->projection, sizeof(F.v.P));
   // Renderer::render, src/Renderer.cpp:317-326.
-  F.persp = f->projection[15] == 0;
-  float zn = F.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
-  F.znear = -zn;
-  F.point = f->light_is_point != 0;
-  if (F.point) affine(f->view, f->light, F.lightdir);
-  else normalized(f->light, F.lightdir);
-  F.ambient = f->ambient;
-  F.lighting = f->lighting != 0;
-  F.save_normals = f->save_normals != 0;
-  memcpy(F.bg, f->background, sizeof(F.bg));
-  F.n_renderables = n;
-  F.n_tris = (uint32_t)total;
+  F.v.persp = f->projection[15] == 0;
+  float zn = F.v.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
+  F.v.znear = -zn;
+  F.v.point = f->light_is_point != 0;
+  if (F.v.point) affine(f->view, f->light, F.v.lightdir);
+  else normalized(f->light, F.v.lightdir);
+  F.v.ambient = f->ambient;
+  F.v.lighting = f->lighting != 0;
+  F.v.save_normals = f->save_normals != 0;
+  memcpy(F.v.bg, f->background, sizeof(F.v.bg));
+  F.g.n_renderables = n;
+  F.g.n_tris = (uint32_t)total;
   F.tile = TS;
   F.tiles_x = tx;
   F.tiles_y = ty;
   F.small_max = c->small_max;
-  F.rs = c->rs.p;
-  F.tri_base = c->tri_base.p;
-  F.vert_base = c->tri_base.p + (n + 1);
-  F.nrm_base = c->tri_base.p + 2 * (n + 1);
-  F.n_verts = (uint32_t)vbase;
-  F.n_nrms = (uint32_t)nbase;
-  F.va = c->va.p;
-  F.vb = c->vb.p;
-  F.vn = c->vn.p;
+  F.g.rs = c->rs.p;
+  F.g.tri_base = c->tri_base.p;
+  F.g.vert_base = c->tri_base.p + (n + 1);
+  F.g.nrm_base = c->tri_base.p + 2 * (n + 1);
+  F.g.n_verts = (uint32_t)vbase;
+  F.g.n_nrms = (uint32_t)nbase;
+  F.g.va = c->va.p;
+  F.g.vb = c->vb.p;
+  F.g.vn = c->vn.p;
   F.vis = c->vis.p;
   F.recs = c->recs.p;
   F.rec_cap = (uint32_t)std::min<size_t>(c->recs.cap, 0xFFFFFFFFu);
@@ -597,7 +650,7 @@ MR_API int mr_read(mr_ctx* c, uint8_t* rgb8, float* depth, float* rgb_f32, uint3
   cudaSetDevice(c->device);
   int rc = settle(c);
   if (rc && rc != MR_E_BAD_INDEX) return rc;
-  size_t npx = (size_t)c->last.W * c->last.H;
+  size_t npx = (size_t)c->last.v.W * c->last.v.H;
   cudaStream_t st = c->stream;
   if (rgb8) {
     if (!c->last.rgb8) return fail(c, MR_E_INVALID, "rgb8 was not requested for this frame");
@@ -627,8 +680,8 @@ MR_API int mr_get_outputs(mr_ctx* c, mr_outputs* o) {
   if (!c || !o) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
   if (!c->have_frame) return fail(c, MR_E_INVALID, "no frame rendered yet");
-  o->width = c->last.W;
-  o->height = c->last.H;
+  o->width = c->last.v.W;
+  o->height = c->last.v.H;
   o->rgb8 = c->last.rgb8;
   o->depth = c->last.depth;
   o->rgb_f32 = c->last.rgbf;
@@ -645,7 +698,7 @@ MR_API int mr_get_stats(mr_ctx* c, mr_stats* s) {
   if (rc && rc != MR_E_BAD_INDEX) return rc;
   memset(s, 0, sizeof(*s));
   const Counters& k = *c->h_cnt;
-  s->triangles = c->last.n_tris;
+  s->triangles = c->last.g.n_tris;
   s->clipped = (int64_t)k.clipped;
   s->rasterised = (int64_t)k.rasterised;
   s->small_direct = (int64_t)k.small_direct;
@@ -666,11 +719,367 @@ MR_API int mr_read_range_image(mr_ctx* c, float* xyz) {
   int rc = settle(c);
   if (rc && rc != MR_E_BAD_INDEX) return rc;
   if (!c->last.depth) return fail(c, MR_E_INVALID, "depth was not requested for this frame");
-  size_t npx = (size_t)c->last.W * c->last.H;
+  size_t npx = (size_t)c->last.v.W * c->last.v.H;
   CK(c->range.ensure(3 * npx), "range buffer");
-  CK(launch_range(c->last.W, c->last.H, c->dP.p, c->last.depth, c->range.p, c->stream), "range launch");
+  CK(launch_range(c->last.v.W, c->last.v.H, c->dP.p, c->last.depth, c->range.p, c->stream), "range launch");
   CK(cudaMemcpyAsync(xyz, c->range.p, 12 * npx, cudaMemcpyDeviceToHost, c->stream), "range read");
   CK(cudaStreamSynchronize(c->stream), "range wait");
+  return rc;
+}
+
+// ------------------------------------------------------------------ batches
+// View of a frame as Renderer::render() prepares it (src/Renderer.cpp:317-326).
+static void make_view(const mr_frame* f, View& V) {
+  memset(&V, 0, sizeof(V));
+  V.W = f->width;
+  V.H = f->height;
+  V.w = (float)f->width;
+  V.h = (float)f->height;
+  memcpy(V.P, f->projection, sizeof(V.P));
+  V.persp = f->projection[15] == 0;
+  float zn = V.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
+  V.znear = -zn;
+  V.point = f->light_is_point != 0;
+  if (V.point) affine(f->view, f->light, V.lightdir);
+  else normalized(f->light, V.lightdir);
+  V.ambient = f->ambient;
+  V.lighting = f->lighting != 0;
+  V.save_normals = f->save_normals != 0;
+  memcpy(V.bg, f->background, sizeof(V.bg));
+}
+
+extern "C++" {
+template <typename T>
+static cudaError_t pinned(T*& p, size_t& cap, size_t n) {
+  if (n <= cap && p) return cudaSuccess;
+  if (p) cudaFreeHost(p);
+  p = nullptr;
+  cap = 0;
+  cudaError_t e = cudaMallocHost(&p, sizeof(T) * std::max<size_t>(n, 1));
+  if (e == cudaSuccess) cap = std::max<size_t>(n, 1);
+  return e;
+}
+}  // extern "C++"
+
+MR_API int mr_set_batch_tuning(mr_ctx* c, int tile, int threads, int chunk) {
+  if (!c) return MR_E_INVALID;
+  if (tile != 8 && tile != 16 && tile != 32) return fail(c, MR_E_INVALID, "tile must be 8, 16 or 32");
+  if (threads != 64 && threads != 128 && threads != 256) return fail(c, MR_E_INVALID, "threads must be 64, 128 or 256");
+  if (chunk < 16 || chunk > 256) return fail(c, MR_E_INVALID, "chunk must be in 16..256");
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  c->b.tile = tile;
+  c->b.threads = threads;
+  c->b.chunk = chunk;
+  return MR_OK;
+}
+
+MR_API int mr_set_batch_graphs(mr_ctx* c, int graphs) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  c->b.graphs = graphs != 0;
+  return MR_OK;
+}
+
+// Enqueues the batch described by c->b (staging already filled).
+static int enqueue_batch(mr_ctx* c, cudaStream_t st) {
+  auto& B = c->b;
+  const int n = B.n_rs, S = B.n_scenes;
+  CK(cudaMemcpyAsync(B.rs.p, B.h_rs, sizeof(DevRenderable) * n, cudaMemcpyHostToDevice, st), "renderable upload");
+  CK(cudaMemcpyAsync(B.bases.p, B.h_u32, sizeof(uint32_t) * (3 * (n + 1) + S + 1), cudaMemcpyHostToDevice, st),
+     "base upload");
+  CK(cudaMemcpyAsync(B.scenes.p, B.h_scenes, sizeof(SceneRec) * S, cudaMemcpyHostToDevice, st), "scene upload");
+  CK(cudaMemsetAsync(B.d_cnt, 0, sizeof(Counters), st), "counter reset");
+  CK(cudaMemsetAsync(B.tiles.p, 0, sizeof(uint32_t) * (3 * (size_t)B.P.n_tiles + 1), st), "tile reset");
+  CK(launch_batch(B.P, B.threads, B.grid, B.block_sums.p, st, c->profiling ? c->ev : nullptr), "batch launch");
+  return MR_OK;
+}
+
+static int run_batch(mr_ctx* c) {
+  auto& B = c->b;
+  std::vector<uint64_t> key = {(uint64_t)B.n_scenes, (uint64_t)B.n_rs, B.P.g.n_tris, B.P.g.n_verts, B.P.g.n_nrms,
+                               (uint64_t)B.tile, (uint64_t)B.threads, (uint64_t)B.chunk, (uint64_t)B.grid,
+                               (uint64_t)c->profiling, (uint64_t)(uintptr_t)c->stream,
+                               (uint64_t)(uintptr_t)B.h_rs, (uint64_t)(uintptr_t)B.h_u32,
+                               (uint64_t)(uintptr_t)B.h_scenes, (uint64_t)(uintptr_t)B.rs.p,
+                               (uint64_t)(uintptr_t)B.bases.p, (uint64_t)(uintptr_t)B.scenes.p,
+                               (uint64_t)(uintptr_t)B.va.p, (uint64_t)(uintptr_t)B.vn.p, (uint64_t)(uintptr_t)B.vb.p,
+                               (uint64_t)(uintptr_t)B.recs.p, (uint64_t)B.P.rec_cap, (uint64_t)(uintptr_t)B.bins.p,
+                               (uint64_t)B.P.bin_cap, (uint64_t)(uintptr_t)B.tiles.p, B.P.n_tiles};
+  for (int s = 0; s < B.n_scenes; s++) {
+    key.push_back(((uint64_t)B.W[s] << 32) | (uint64_t)B.H[s]);
+    key.push_back((uint64_t)(uintptr_t)B.h_scenes[s].rgb8 ^ ((uint64_t)(uintptr_t)B.h_scenes[s].depth << 1) ^
+                  ((uint64_t)(uintptr_t)B.h_scenes[s].ids << 2));
+  }
+  cudaStream_t st = c->stream;
+  if (!B.graphs) return enqueue_batch(c, st);
+  if (!B.exec || key != B.key) {
+    if (B.exec) cudaGraphExecDestroy(B.exec);
+    if (B.graph) cudaGraphDestroy(B.graph);
+    B.exec = nullptr;
+    B.graph = nullptr;
+    B.key.clear();
+    CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
+    int rc = enqueue_batch(c, st);
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamEndCapture(st, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    CK(e, "end capture");
+    B.graph = g;
+    CK(cudaGraphInstantiate(&B.exec, g, 0), "graph instantiate");
+    B.key = key;
+  }
+  CK(cudaGraphLaunch(B.exec, st), "graph launch");
+  return MR_OK;
+}
+
+MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes, const mr_renderable* rs,
+                           int32_t n_rs, int32_t outputs) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  if (!sc || n_scenes <= 0 || n_rs < 0 || (n_rs > 0 && !rs)) return fail(c, MR_E_INVALID, "bad batch");
+  auto& B = c->b;
+  cudaSetDevice(c->device);
+  // validate scenes and renderable ranges
+  uint64_t tris = 0, verts = 0, nrms = 0, pixels = 0, tiles = 0;
+  const int TS = B.tile;
+  for (int32_t s = 0; s < n_scenes; s++) {
+    const mr_frame* f = &sc[s].frame;
+    if (f->width <= 0 || f->height <= 0 || f->width > (1 << 16) || f->height > (1 << 16))
+      return fail(c, MR_E_INVALID, "scene frame size out of range");
+    if (sc[s].first_renderable < 0 || sc[s].n_renderables < 0 ||
+        (int64_t)sc[s].first_renderable + sc[s].n_renderables > n_rs ||
+        (s > 0 && sc[s].first_renderable != sc[s - 1].first_renderable + sc[s - 1].n_renderables) ||
+        (s == 0 && sc[s].first_renderable != 0))
+      return fail(c, MR_E_INVALID, "scene renderable ranges must tile the renderable array in order");
+    pixels += (uint64_t)f->width * f->height;
+    tiles += (uint64_t)((f->width + TS - 1) / TS) * ((f->height + TS - 1) / TS);
+  }
+  if (sc[n_scenes - 1].first_renderable + sc[n_scenes - 1].n_renderables != n_rs)
+    return fail(c, MR_E_INVALID, "scene renderable ranges must cover every renderable");
+  for (int32_t i = 0; i < n_rs; i++) {
+    int32_t h = rs[i].mesh;
+    if (h < 0 || h >= (int32_t)c->meshes.size() || !c->meshes[h].live)
+      return fail(c, MR_E_HANDLE, "renderable refers to an unknown mesh");
+    int32_t t = rs[i].material.texture;
+    if (t >= 0 && (t >= (int32_t)c->textures.size() || !c->textures[t].live))
+      return fail(c, MR_E_HANDLE, "material refers to an unknown texture");
+    tris += (uint64_t)c->meshes[h].d.n_tri;
+    verts += (uint64_t)c->meshes[h].d.n_pos;
+    nrms += (uint64_t)c->meshes[h].d.n_nrm;
+  }
+  if (tris >= ((uint64_t)1 << 31) || verts >= ((uint64_t)1 << 32) || nrms >= ((uint64_t)1 << 32) ||
+      tiles >= ((uint64_t)1 << 31))
+    return fail(c, MR_E_INVALID, "batch too large for 32-bit indices");
+  // staging (wait until the previous batch has consumed it)
+  CK(cudaEventSynchronize(B.done), "staging wait");
+  CK(pinned(B.h_rs, B.h_rs_cap, (size_t)n_rs), "pinned staging");
+  CK(pinned(B.h_u32, B.h_u32_cap, (size_t)3 * (n_rs + 1) + n_scenes + 1), "pinned staging");
+  CK(pinned(B.h_scenes, B.h_scenes_cap, (size_t)n_scenes), "pinned staging");
+  uint32_t* tb = B.h_u32;
+  uint32_t* vbase = tb + (n_rs + 1);
+  uint32_t* nbase = tb + 2 * (n_rs + 1);
+  uint32_t* stb = tb + 3 * (n_rs + 1);
+  // outputs pool
+  B.W.assign(n_scenes, 0);
+  B.H.assign(n_scenes, 0);
+  B.px_off.assign(n_scenes + 1, 0);
+  for (int32_t s = 0; s < n_scenes; s++) {
+    B.W[s] = sc[s].frame.width;
+    B.H[s] = sc[s].frame.height;
+    B.px_off[s + 1] = B.px_off[s] + (size_t)B.W[s] * B.H[s];
+  }
+  if (outputs & MR_OUT_RGB8) CK(B.out8.ensure(3 * pixels), "batch rgb8");
+  if (outputs & MR_OUT_DEPTH) CK(B.outd.ensure(pixels), "batch depth");
+  if (outputs & MR_OUT_TRI_ID) CK(B.outi.ensure(pixels), "batch ids");
+  CK(B.rs.ensure((size_t)n_rs), "batch renderables");
+  CK(B.bases.ensure((size_t)3 * (n_rs + 1) + n_scenes + 1), "batch bases");
+  CK(B.scenes.ensure((size_t)n_scenes), "batch scenes");
+  CK(B.va.ensure(verts), "batch vertex buffer");
+  CK(B.vb.ensure(verts), "batch vertex buffer");
+  CK(B.vn.ensure(nrms), "batch normal buffer");
+  CK(B.recs.ensure(2 * tris), "batch records");
+  CK(B.rec_scene.ensure(2 * tris), "batch records");
+  CK(B.tiles.ensure(3 * tiles + 1), "batch tiles");
+  if (B.bins.cap < std::max<size_t>((size_t)1 << 20, 2 * tris)) CK(B.bins.ensure(std::max<size_t>((size_t)1 << 20, 2 * tris)), "batch bins");
+  int grid = batch_grid(B.tile, B.chunk, B.threads);
+  if (grid <= 0) return fail(c, MR_E_INVALID, "batch tuning does not fit on the device");
+  CK(B.block_sums.ensure((size_t)grid + 1), "batch scan");
+  // renderables, bases and scenes
+  uint32_t tri = 0, vb = 0, nb = 0, tile_base = 0;
+  for (int32_t s = 0; s < n_scenes; s++) {
+    const mr_frame* f = &sc[s].frame;
+    SceneRec& SR = B.h_scenes[s];
+    memset(&SR, 0, sizeof(SR));
+    make_view(f, SR.v);
+    SR.tiles_x = (f->width + TS - 1) / TS;
+    SR.tiles_y = (f->height + TS - 1) / TS;
+    SR.tile_base = tile_base;
+    stb[s] = tile_base;
+    tile_base += (uint32_t)(SR.tiles_x * SR.tiles_y);
+    SR.rs_begin = (uint32_t)sc[s].first_renderable;
+    SR.rs_end = (uint32_t)(sc[s].first_renderable + sc[s].n_renderables);
+    SR.rgb8 = (outputs & MR_OUT_RGB8) ? B.out8.p + 3 * B.px_off[s] : nullptr;
+    SR.depth = (outputs & MR_OUT_DEPTH) ? B.outd.p + B.px_off[s] : nullptr;
+    SR.ids = (outputs & MR_OUT_TRI_ID) ? B.outi.p + B.px_off[s] : nullptr;
+    for (int32_t i = sc[s].first_renderable; i < sc[s].first_renderable + sc[s].n_renderables; i++) {
+      const MeshRec& m = c->meshes[rs[i].mesh];
+      DevRenderable& R = B.h_rs[i];
+      memset(&R, 0, sizeof(R));
+      float mv[16], inv[16], nm[16];
+      mat4_mul(f->view, rs[i].transform, mv);
+      mat4_inverse(mv, inv);
+      mat4_transpose(inv, nm);
+      memcpy(R.mv, mv, sizeof(R.mv));
+      memcpy(R.nm, nm, sizeof(R.nm));
+      R.mesh = m.d;
+      R.tri_base = tri;
+      R.vert_base = vb;
+      R.nrm_base = nb;
+      R.scene = (uint32_t)s;
+      tb[i] = tri;
+      vbase[i] = vb;
+      nbase[i] = nb;
+      tri += (uint32_t)m.d.n_tri;
+      vb += (uint32_t)m.d.n_pos;
+      nb += (uint32_t)m.d.n_nrm;
+      const mr_material& M = rs[i].material;
+      memcpy(R.diffuse, M.diffuse, sizeof(R.diffuse));
+      memcpy(R.specular, M.specular, sizeof(R.specular));
+      memcpy(R.emissive, M.emissive, sizeof(R.emissive));
+      R.shininess = M.shininess;
+      if (f->texturing && M.texture >= 0) {
+        const TexRec& T = c->textures[M.texture];
+        R.has_tex = 1;
+        R.tex_rows = T.rows;
+        R.tex_cols = T.cols;
+        if (T.rgb8) R.tex8 = (const uint8_t*)T.mem;
+        else R.texf = (const float*)T.mem;
+      }
+    }
+  }
+  tb[n_rs] = tri;
+  vbase[n_rs] = vb;
+  nbase[n_rs] = nb;
+  stb[n_scenes] = tile_base;
+  BatchParams& P = B.P;
+  memset(&P, 0, sizeof(P));
+  P.g.rs = B.rs.p;
+  P.g.tri_base = B.bases.p;
+  P.g.vert_base = B.bases.p + (n_rs + 1);
+  P.g.nrm_base = B.bases.p + 2 * (n_rs + 1);
+  P.g.n_renderables = n_rs;
+  P.g.n_tris = tri;
+  P.g.n_verts = vb;
+  P.g.n_nrms = nb;
+  P.g.va = B.va.p;
+  P.g.vb = B.vb.p;
+  P.g.vn = B.vn.p;
+  P.scenes = B.scenes.p;
+  P.scene_tile_base = B.bases.p + 3 * (n_rs + 1);
+  P.n_scenes = n_scenes;
+  P.n_tiles = tile_base;
+  P.tile = TS;
+  P.chunk = B.chunk;
+  P.recs = B.recs.p;
+  P.rec_cap = (uint32_t)std::min<size_t>(B.recs.cap, 0xFFFFFFFFu);
+  P.rec_scene = B.rec_scene.p;
+  P.tile_count = B.tiles.p;
+  P.tile_fill = B.tiles.p + tile_base;
+  P.tile_start = B.tiles.p + 2 * (size_t)tile_base;
+  P.bins = B.bins.p;
+  P.bin_cap = (uint32_t)std::min<size_t>(B.bins.cap, 0xFFFFFFFFu);
+  P.counters = B.d_cnt;
+  B.grid = grid;
+  B.n_scenes = n_scenes;
+  B.n_rs = n_rs;
+  int rc = run_batch(c);
+  if (rc) return rc;
+  CK(cudaEventRecord(B.done, c->stream), "batch event");
+  B.have = true;
+  return MR_OK;
+}
+
+// Waits for the last batch; re-runs it while the bin list overflowed.
+static int settle_batch(mr_ctx* c) {
+  auto& B = c->b;
+  if (!B.have) return fail(c, MR_E_INVALID, "no batch rendered yet");
+  for (int attempt = 0; attempt < 8; attempt++) {
+    CK(cudaMemcpyAsync(B.h_cnt, B.d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "counter read");
+    CK(cudaStreamSynchronize(c->stream), "batch wait");
+    if (!B.h_cnt->bin_overflow)
+      return (B.h_cnt->error_flags & 1u) ? fail(c, MR_E_BAD_INDEX, "a mesh index was out of range; those triangles were skipped") : MR_OK;
+    size_t want = (size_t)B.h_cnt->bin_needed + B.h_cnt->bin_needed / 4 + 1024;
+    CK(B.bins.ensure(want), "batch bins");
+    B.P.bins = B.bins.p;
+    B.P.bin_cap = (uint32_t)std::min<size_t>(B.bins.cap, 0xFFFFFFFFu);
+    int rc = run_batch(c);
+    if (rc) return rc;
+  }
+  return fail(c, MR_E_NOMEM, "bin list kept overflowing");
+}
+
+MR_API int mr_read_batch(mr_ctx* c, int32_t s, uint8_t* rgb8, float* depth, uint32_t* ids) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  int rc = settle_batch(c);
+  if (rc && rc != MR_E_BAD_INDEX) return rc;
+  auto& B = c->b;
+  if (s < 0 || s >= B.n_scenes) return fail(c, MR_E_INVALID, "scene index out of range");
+  size_t npx = (size_t)B.W[s] * B.H[s];
+  const SceneRec& SR = B.h_scenes[s];
+  cudaStream_t st = c->stream;
+  if (rgb8) {
+    if (!SR.rgb8) return fail(c, MR_E_INVALID, "rgb8 was not requested for this batch");
+    CK(cudaMemcpyAsync(rgb8, SR.rgb8, 3 * npx, cudaMemcpyDeviceToHost, st), "rgb8 read");
+  }
+  if (depth) {
+    if (!SR.depth) return fail(c, MR_E_INVALID, "depth was not requested for this batch");
+    CK(cudaMemcpyAsync(depth, SR.depth, 4 * npx, cudaMemcpyDeviceToHost, st), "depth read");
+  }
+  if (ids) {
+    if (!SR.ids) return fail(c, MR_E_INVALID, "ids were not requested for this batch");
+    CK(cudaMemcpyAsync(ids, SR.ids, 4 * npx, cudaMemcpyDeviceToHost, st), "id read");
+  }
+  CK(cudaStreamSynchronize(st), "read wait");
+  return rc;
+}
+
+MR_API int mr_get_batch_outputs(mr_ctx* c, int32_t s, mr_outputs* o) {
+  if (!c || !o) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  auto& B = c->b;
+  if (!B.have || s < 0 || s >= B.n_scenes) return fail(c, MR_E_INVALID, "no such scene in the last batch");
+  memset(o, 0, sizeof(*o));
+  o->width = B.W[s];
+  o->height = B.H[s];
+  o->rgb8 = B.h_scenes[s].rgb8;
+  o->depth = B.h_scenes[s].depth;
+  o->tri_id = B.h_scenes[s].ids;
+  return MR_OK;
+}
+
+MR_API int mr_get_batch_stats(mr_ctx* c, mr_stats* s) {
+  if (!c || !s) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  int rc = settle_batch(c);
+  if (rc && rc != MR_E_BAD_INDEX) return rc;
+  memset(s, 0, sizeof(*s));
+  const Counters& k = *c->b.h_cnt;
+  s->triangles = c->b.P.g.n_tris;
+  s->clipped = (int64_t)k.clipped;
+  s->rasterised = (int64_t)k.rasterised;
+  s->binned = (int64_t)k.rec_count;
+  s->bin_entries = (int64_t)k.bin_needed;
+  s->error_flags = k.error_flags;
+  if (c->profiling) {
+    s->n_stages = 3;
+    for (int i = 0; i < 3; i++) cudaEventElapsedTime(&s->stage_ms[i], c->ev[i], c->ev[i + 1]);
+  }
   return rc;
 }
 

@@ -1,7 +1,7 @@
-// GB300 (sm_103a) kernels of the one-frame-per-call rasterisation path.
+// GB300 (sm_103a) kernels of the rasterisation path.
 //
+// One frame per call (launch_frame):
 //   k_clear        vis[] = VIS_EMPTY                 (Renderer::clear, src/Renderer.cpp:113-119)
-//   k_validate     per-mesh bad-triangle bitmask     (index checks done once at upload)
 //   k_vertex       per-vertex view transform + projection to pixel space and
 //                  per-normal transform, once per frame (the PREMULT loops,
 //                  src/Renderer.cpp:344-348, plus htransform :13-20 and the
@@ -17,18 +17,22 @@
 //   k_resolve      deferred pass: re-derives the winning sub-triangle's
 //                  barycentrics exactly, shades once per visible pixel and
 //                  writes RGB8/depth/ids            (src/Renderer.cpp:271-305, src/io.cpp:358-362)
-//   k_range        getRangeImage                      (src/Renderer.cpp:388-415)
+// Many frames per call (launch_batch):
+//   k_vertex, then k_setup_batch (every rasterised sub-triangle becomes a
+//   record, counted into its scene's tiles), then k_batch: one cooperative,
+//   persistent launch -- scan, scatter, and a dynamically scheduled loop over
+//   all tiles of all scenes that rasterises each tile into shared memory and
+//   resolves + shades its pixels in place (no frame-sized visibility buffer).
+// Also: k_validate (index checks at upload), k_range (getRangeImage,
+// src/Renderer.cpp:388-415).
 //
-// Exactness: every float operation follows the reference's order; the
-// edge functions are advanced column by column from the bounding-box edge
-// exactly as the reference loop does (the running sums have no closed form),
-// so both the rasterisers and the resolve pass replay that chain.  Values the
-// vertex pass stores are the same expressions the reference evaluates per
-// triangle corner, so storing them changes no bit.
-//
-// Kernels templated on PRE use the vertex-pass buffers when PRE is true and
-// transform vertices per triangle otherwise (the allocation-free entry point
-// has no room for per-vertex buffers).
+// Exactness: every float operation follows the reference's order; the edge
+// functions are advanced column by column from the bounding-box edge exactly
+// as the reference loop does (the running sums have no closed form), so every
+// rasteriser and the resolve replay that chain.  Values the vertex pass stores
+// are the same expressions the reference evaluates per triangle corner.
+// Kernels templated on PRE read the vertex-pass buffers; without them
+// (allocation-free entry point) vertices are transformed per triangle.
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
@@ -39,8 +43,7 @@ namespace cg = cooperative_groups;
 namespace mrg {
 
 // ------------------------------------------------------------------ helpers
-__device__ __forceinline__ int find_base(const uint32_t* base, int n, uint32_t g) {
-  int lo = 0, hi = n;
+__device__ __forceinline__ int find_base(const uint32_t* base, int lo, int hi, uint32_t g) {
   while (hi - lo > 1) {
     int mid = (lo + hi) >> 1;
     if (base[mid] <= g) lo = mid; else hi = mid;
@@ -64,11 +67,11 @@ __device__ __forceinline__ V3 htransform(const float* m, V3 p) {
 }
 
 // Pixel coordinates and depth term of one corner, src/Renderer.cpp:186-197, 223-224.
-__device__ __forceinline__ void project(const FrameParams& F, V3 v, float& px, float& py, float& zt) {
-  V3 ndc = htransform(F.P, v);
-  px = (1 + ndc.x) * (F.w / 2);
-  py = (1 - ndc.y) * (F.h / 2);
-  zt = F.persp ? -rcp(v.z) : ndc.z;
+__device__ __forceinline__ void project(const View& V, V3 v, float& px, float& py, float& zt) {
+  V3 ndc = htransform(V.P, v);
+  px = (1 + ndc.x) * (V.w / 2);
+  py = (1 - ndc.y) * (V.h / 2);
+  zt = V.persp ? -rcp(v.z) : ndc.z;
 }
 
 // clip(), src/Renderer.cpp:121-129
@@ -115,14 +118,14 @@ __device__ __forceinline__ int clip_tri(float zn, Vtx (&v)[3], Vtx (&sub)[2][3])
 
 // View-space corners of triangle t (paintMesh, src/Renderer.cpp:344-379).
 template <bool PRE, bool ATTR>
-__device__ __forceinline__ void corners(const FrameParams& F, const DevRenderable& R, int t,
-                                        const int (&ip)[3], Vtx (&v)[3]) {
+__device__ __forceinline__ void corners(const Geo& G, const DevRenderable& R, int t, const int (&ip)[3],
+                                        Vtx (&v)[3]) {
   const DevMesh& M = R.mesh;
 #pragma unroll
   for (int c = 0; c < 3; c++) {
     if (PRE) {
-      float4 a = F.va[R.vert_base + ip[c]];
-      float2 b = F.vb[R.vert_base + ip[c]];
+      float4 a = G.va[R.vert_base + ip[c]];
+      float2 b = G.vb[R.vert_base + ip[c]];
       v[c].pos = v3(b.x, b.y, a.w);
     } else {
       v[c].pos = affine(R.mv, ld3(M.pos, ip[c]));
@@ -130,7 +133,7 @@ __device__ __forceinline__ void corners(const FrameParams& F, const DevRenderabl
     if (ATTR) {
       int in = __ldg(M.nidx + 3 * t + c);
       if (PRE) {
-        float4 n = F.vn[R.nrm_base + in];
+        float4 n = G.vn[R.nrm_base + in];
         v[c].nrm = v3(n.x, n.y, n.z);
       } else {
         v[c].nrm = affine(R.nm, ld3(M.nrm, in));
@@ -148,15 +151,14 @@ struct Setup {
 
 // paintTriangle setup from projected corners, src/Renderer.cpp:198-224.
 // False = nothing to draw (off screen or culled).
-__device__ __forceinline__ bool setup_from(const FrameParams& F, const V2 (&p)[3], const float (&zt)[3],
-                                           Setup& S) {
+__device__ __forceinline__ bool setup_from(const View& V, const V2 (&p)[3], const float (&zt)[3], Setup& S) {
   V2 pmin = v2(1e30f, 1e30f), pmax = v2(-1e30f, -1e30f);
 #pragma unroll
   for (int i = 0; i < 3; i++) {
     pmin = v2(minr(pmin.x, p[i].x), minr(pmin.y, p[i].y));
     pmax = v2(maxr(pmax.x, p[i].x), maxr(pmax.y, p[i].y));
   }
-  if (pmax.x < 0 || pmax.y < 0 || pmin.x > F.w || pmin.y > F.h) return false;
+  if (pmax.x < 0 || pmax.y < 0 || pmin.x > V.w || pmin.y > V.h) return false;
   float d0x = p[0].x - p[1].x, d0y = p[0].y - p[1].y;
   float d2x = p[2].x - p[1].x, d2y = p[2].y - p[1].y;
   float a = d0x * d2y - d0y * d2x;
@@ -167,10 +169,10 @@ __device__ __forceinline__ bool setup_from(const FrameParams& F, const V2 (&p)[3
   ex = p[1].x - p[0].x;
   ey = p[1].y - p[0].y;
   S.n2 = v2(-ey * i2a, ex * i2a);
-  pmin.x = clampr(pmin.x, 0.f, F.w - 1);
-  pmax.x = clampr(pmax.x, 0.f, F.w - 1);
-  pmin.y = clampr(pmin.y, 0.f, F.h - 1);
-  pmax.y = clampr(pmax.y, 0.f, F.h - 1);
+  pmin.x = clampr(pmin.x, 0.f, V.w - 1);
+  pmax.x = clampr(pmax.x, 0.f, V.w - 1);
+  pmin.y = clampr(pmin.y, 0.f, V.h - 1);
+  pmax.y = clampr(pmax.y, 0.f, V.h - 1);
   S.x0 = (int)floorf(pmin.x);
   S.y0 = (int)floorf(pmin.y);
   S.x1 = (int)floorf(pmax.x);
@@ -184,12 +186,12 @@ __device__ __forceinline__ bool setup_from(const FrameParams& F, const V2 (&p)[3
 }
 
 // Setup of a sub-triangle given by view-space corners (the clipped path).
-__device__ __forceinline__ bool setup_view(const FrameParams& F, const Vtx (&s)[3], Setup& S) {
+__device__ __forceinline__ bool setup_view(const View& V, const Vtx (&s)[3], Setup& S) {
   V2 p[3];
   float zt[3];
 #pragma unroll
-  for (int i = 0; i < 3; i++) project(F, s[i].pos, p[i].x, p[i].y, zt[i]);
-  return setup_from(F, p, zt, S);
+  for (int i = 0; i < 3; i++) project(V, s[i].pos, p[i].x, p[i].y, zt[i]);
+  return setup_from(V, p, zt, S);
 }
 
 // Edge functions at the start of row y (pixel centre x0+0.5), :240-242.
@@ -270,6 +272,135 @@ __device__ __forceinline__ Setup rec_setup(const BigRec& B) {
   return S;
 }
 
+// Assembly, near clip and setup of global triangle g (paintMesh + the first
+// half of paintTriangle).  Fills up to two setups in draw order; kind[s] = 1
+// for a sub-triangle with pixels to test.  Returns false for a triangle whose
+// indices failed the upload check.
+template <bool PRE>
+__device__ __forceinline__ bool setup_triangle(const View& V, const Geo& G, const DevRenderable& R,
+                                               uint32_t g, Setup (&S)[2], int (&kind)[2],
+                                               unsigned& n_clipped) {
+  const int t = (int)(g - R.tri_base);
+  if ((R.mesh.bad[t >> 5] >> (t & 31)) & 1u) return false;
+  int ip[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) ip[c] = __ldg(R.mesh.idx + 3 * t + c);
+  const float zn = V.znear;
+  if (PRE) {
+    float4 a[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) a[c] = G.va[R.vert_base + ip[c]];
+    if (!(a[0].w > zn || a[1].w > zn || a[2].w > zn)) {
+      V2 p[3] = {v2(a[0].x, a[0].y), v2(a[1].x, a[1].y), v2(a[2].x, a[2].y)};
+      float zt[3] = {a[0].z, a[1].z, a[2].z};
+      if (setup_from(V, p, zt, S[0])) kind[0] = 1;
+      return true;
+    }
+  }
+  Vtx v[3], sub[2][3];
+  corners<PRE, false>(G, R, t, ip, v);
+  int n;
+  if (!(v[0].pos.z > zn || v[1].pos.z > zn || v[2].pos.z > zn)) {
+    sub[0][0] = v[0]; sub[0][1] = v[1]; sub[0][2] = v[2];
+    n = 1;
+  } else {
+    n = clip_tri<false>(zn, v, sub);
+    n_clipped += n > 0;
+  }
+  for (int s = 0; s < n; s++)
+    if (setup_view(V, sub[s], S[s])) kind[s] = 1;
+  return true;
+}
+
+// Shading of the pixel (x, y) whose visibility word is vw, src/Renderer.cpp:
+// 247-305 (FAST_LIGHT): re-derives the winner's setup, replays its edge
+// functions to column x, and evaluates texture and Blinn-Phong lighting.
+// Renderables of the pixel's frame are rs_lo..rs_hi-1.
+template <bool PRE>
+__device__ __forceinline__ void resolve_pixel(const View& V, const Geo& G, int rs_lo, int rs_hi,
+                                              unsigned long long vw, int x, int y, const float* s_dec,
+                                              V3& value, float& depth, uint32_t& id, V3& normal_out) {
+  normal_out = v3(0, 0, 1);
+  if (vw == VIS_EMPTY) {
+    value = v3(V.bg[0], V.bg[1], V.bg[2]);
+    depth = 1e11f;
+    id = MR_NO_TRIANGLE;
+    return;
+  }
+  id = (uint32_t)vw;
+  const uint32_t g = id >> 1;
+  const int s = (int)(id & 1u);
+  const DevRenderable& R = G.rs[find_base(G.tri_base, rs_lo, rs_hi, g)];
+  const int t = (int)(g - R.tri_base);
+  int ip[3];
+#pragma unroll
+  for (int c = 0; c < 3; c++) ip[c] = __ldg(R.mesh.idx + 3 * t + c);
+  Vtx vc[3];
+  corners<PRE, true>(G, R, t, ip, vc);
+  Setup S;
+  const float zn = V.znear;
+  if (vc[0].pos.z > zn || vc[1].pos.z > zn || vc[2].pos.z > zn) {
+    Vtx sub[2][3];
+    clip_tri<true>(zn, vc, sub);
+    // sub-triangle s exists: it won this pixel
+#pragma unroll
+    for (int c = 0; c < 3; c++) vc[c] = s ? sub[1][c] : sub[0][c];
+    setup_view(V, vc, S);
+  } else if (PRE) {
+    V2 p[3];
+    float zt[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float4 a = G.va[R.vert_base + ip[c]];
+      p[c] = v2(a.x, a.y);
+      zt[c] = a.z;
+    }
+    setup_from(V, p, zt, S);
+  } else {
+    setup_view(V, vc, S);
+  }
+  float e1, e2;
+  row_start(S, y, e1, e2);
+  for (int c = S.x0; c < x; c++) {
+    e1 += S.n1.x;
+    e2 += S.n2.x;
+  }
+  float k0, k1, k2;
+  depth = frag_depth(S, V.persp != 0, e1, e2, k0, k1, k2);
+  V3 color = v3(R.diffuse[0], R.diffuse[1], R.diffuse[2]);
+  if (R.has_tex) {
+    V2 uv = add2(add2(ks2(k0, vc[0].uv), ks2(k1, vc[1].uv)), ks2(k2, vc[2].uv));
+    int ti = (int)((uv.y - floorf(uv.y)) * (float)R.tex_rows);
+    int tj = (int)((uv.x - floorf(uv.x)) * (float)R.tex_cols);
+    ti = min(max(ti, 0), R.tex_rows - 1);
+    tj = min(max(tj, 0), R.tex_cols - 1);
+    size_t o = 3 * ((size_t)ti * R.tex_cols + tj);
+    if (R.tex8)
+      color = v3(s_dec[R.tex8[o]], s_dec[R.tex8[o + 1]], s_dec[R.tex8[o + 2]]);
+    else
+      color = v3(R.texf[o], R.texf[o + 1], R.texf[o + 2]);
+  }
+  value = v3(R.emissive[0], R.emissive[1], R.emissive[2]);
+  if (V.lighting) {
+    V3 position = add3(add3(ks3(k0, vc[0].pos), ks3(k1, vc[1].pos)), ks3(k2, vc[2].pos));
+    V3 LD = v3(V.lightdir[0], V.lightdir[1], V.lightdir[2]);
+    V3 lightdir = V.point ? normalized3(sub3(LD, position)) : LD;
+    V3 normal = add3(add3(ks3(k0, vc[0].nrm), ks3(k1, vc[1].nrm)), ks3(k2, vc[2].nrm));
+    float sdiff = maxr(0.0f, dot3(normal, lightdir)) / len3(normal) + V.ambient;
+    value = add3(value, ks3(sdiff, color));
+    if (R.shininess != 0) {
+      V3 viewDir = normalized3(position);
+      V3 lv = sub3(lightdir, viewDir);
+      float spec = powf(maxr(dot3(lv, normal), 0.0f) / (len3(lv) * len3(normal)), R.shininess);
+      value = add3(value, ks3(spec, v3(R.specular[0], R.specular[1], R.specular[2])));
+    }
+    normal_out = normal;
+  }
+}
+
+// savePPM conversion, src/io.cpp:358-362.
+__device__ __forceinline__ uint8_t to_byte(float v) { return (uint8_t)(int)clampr(v * 255.0f, 0.0f, 255.0f); }
+
 // ------------------------------------------------------------------ kernels
 __global__ void k_clear(unsigned long long* vis, size_t n) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -295,23 +426,22 @@ __global__ void k_validate(DevMesh M, uint32_t* bad) {
 }
 
 // Vertex pass: threads [0, n_verts) transform and project positions,
-// threads [n_verts, n_verts + n_nrms) transform normals.
-__global__ void __launch_bounds__(256) k_vertex(FrameParams F) {
+// threads [n_verts, n_verts + n_nrms) transform normals.  The view of a
+// vertex is scenes[R.scene].v for batches, V otherwise.
+__global__ void __launch_bounds__(256) k_vertex(Geo G, View V, const SceneRec* scenes) {
   uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  if (g < F.n_verts) {
-    int r = find_base(F.vert_base, F.n_renderables, g);
-    const DevRenderable& R = F.rs[r];
+  if (g < G.n_verts) {
+    const DevRenderable& R = G.rs[find_base(G.vert_base, 0, G.n_renderables, g)];
     V3 v = affine(R.mv, ld3(R.mesh.pos, (int)(g - R.vert_base)));
     float px, py, zt;
-    project(F, v, px, py, zt);
-    F.va[g] = make_float4(px, py, zt, v.z);
-    F.vb[g] = make_float2(v.x, v.y);
-  } else if (g - F.n_verts < F.n_nrms) {
-    uint32_t gn = g - F.n_verts;
-    int r = find_base(F.nrm_base, F.n_renderables, gn);
-    const DevRenderable& R = F.rs[r];
+    project(scenes ? scenes[R.scene].v : V, v, px, py, zt);
+    G.va[g] = make_float4(px, py, zt, v.z);
+    G.vb[g] = make_float2(v.x, v.y);
+  } else if (g - G.n_verts < G.n_nrms) {
+    uint32_t gn = g - G.n_verts;
+    const DevRenderable& R = G.rs[find_base(G.nrm_base, 0, G.n_renderables, gn)];
     V3 n = affine(R.nm, ld3(R.mesh.nrm, (int)(gn - R.nrm_base)));
-    F.vn[gn] = make_float4(n.x, n.y, n.z, 0.f);
+    G.vn[gn] = make_float4(n.x, n.y, n.z, 0.f);
   }
 }
 
@@ -332,53 +462,19 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
-  const bool persp = F.persp != 0;
+  const bool persp = F.v.persp != 0;
   Setup S[2];
   int kind[2] = {0, 0};  // 0 none, 1 small, 2 big
   unsigned n_clipped = 0, n_raster = 0, n_small = 0;
-  if (g < F.n_tris) {
-    int r = find_base(F.tri_base, F.n_renderables, g);
-    const DevRenderable& R = F.rs[r];
-    const int t = (int)(g - R.tri_base);
-    if ((R.mesh.bad[t >> 5] >> (t & 31)) & 1u) {
+  if (g < F.g.n_tris) {
+    const DevRenderable& R = F.g.rs[find_base(F.g.tri_base, 0, F.g.n_renderables, g)];
+    if (!setup_triangle<PRE>(F.v, F.g, R, g, S, kind, n_clipped)) {
       atomicOr(&F.counters->error_flags, 1u);
     } else {
-      int ip[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) ip[c] = __ldg(R.mesh.idx + 3 * t + c);
-      const float zn = F.znear;
-      int n = 0;
-      if (PRE) {
-        float4 a[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) a[c] = F.va[R.vert_base + ip[c]];
-        if (!(a[0].w > zn || a[1].w > zn || a[2].w > zn)) {
-          V2 p[3] = {v2(a[0].x, a[0].y), v2(a[1].x, a[1].y), v2(a[2].x, a[2].y)};
-          float zt[3] = {a[0].z, a[1].z, a[2].z};
-          if (setup_from(F, p, zt, S[0])) { kind[0] = 1; n_raster++; }
-        } else {
-          n = -1;  // clipped below
-        }
-      } else {
-        n = -1;
-      }
-      if (n < 0) {
-        Vtx v[3], sub[2][3];
-        corners<PRE, false>(F, R, t, ip, v);
-        bool any = v[0].pos.z > zn || v[1].pos.z > zn || v[2].pos.z > zn;
-        if (!any) {
-          sub[0][0] = v[0]; sub[0][1] = v[1]; sub[0][2] = v[2];
-          n = 1;
-        } else {
-          n = clip_tri<false>(zn, v, sub);
-          n_clipped += n > 0;
-        }
-        for (int s = 0; s < n; s++)
-          if (setup_view(F, sub[s], S[s])) { kind[s] = 1; n_raster++; }
-      }
 #pragma unroll
       for (int s = 0; s < 2; s++)
         if (kind[s]) {
+          n_raster++;
           long long bw = S[s].x1 - S[s].x0 + 1, bh = S[s].y1 - S[s].y0 + 1;
           if (bw * bh <= (long long)F.small_max) n_small++;
           else kind[s] = 2;
@@ -431,7 +527,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
     __syncwarp();
     const int total = tot0 + tot1;
     unsigned long long* vis = F.vis;
-    const int W = F.W;
+    const int W = F.v.W;
     for (int b = 0; b < total; b += 32) {
       int k = b + (int)lane;
       if (k < total) {
@@ -458,30 +554,22 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
   warp_add(&F.counters->clipped, n_clipped);
 }
 
-__device__ __forceinline__ void rec_tiles(const FrameParams& F, const BigRec& B, int& tx0, int& ty0,
-                                          int& tx1, int& ty1) {
-  tx0 = B.x0 / F.tile; tx1 = B.x1 / F.tile;
-  ty0 = B.y0 / F.tile; ty1 = B.y1 / F.tile;
+__device__ __forceinline__ void rec_tiles(int tile, const BigRec& B, int& tx0, int& ty0, int& tx1, int& ty1) {
+  tx0 = B.x0 / tile; tx1 = B.x1 / tile;
+  ty0 = B.y0 / tile; ty1 = B.y1 / tile;
 }
 
-// Rasterises the binned (record, row) pairs of one tile into a shared-memory
-// visibility tile, then merges it into vis[] with 64-bit atomicMin.  Called
-// by every thread of the block.
-__device__ __forceinline__ void tile_raster(const FrameParams& F, int tile, unsigned long long* svis) {
-  const int TS = F.tile;
-  uint32_t s = F.tile_start[tile], e = min(F.tile_start[tile + 1], F.bin_cap);
-  if (s >= e) return;  // uniform across the block
-  const int tx = tile % F.tiles_x, ty = tile / F.tiles_x;
-  const int px0 = tx * TS, py0 = ty * TS;
-  const int px1 = min(px0 + TS, F.W) - 1, py1 = min(py0 + TS, F.H) - 1;
-  for (int i = threadIdx.x; i < TS * TS; i += blockDim.x) svis[i] = VIS_EMPTY;
-  __syncthreads();
-  const bool persp = F.persp != 0;
+// Rasterises the (record, row) pairs of records recs[bins[s..e)] that fall in
+// the tile at (px0, py0) into the shared-memory visibility tile svis (bins
+// null: records s..e directly).  Called by every thread of the block.
+__device__ __forceinline__ void raster_into_tile(const BigRec* recs, const uint32_t* bins, uint32_t s,
+                                                 uint32_t e, int TS, int px0, int py0, int px1, int py1,
+                                                 bool persp, unsigned long long* svis) {
   const uint32_t work = (e - s) * (uint32_t)TS;
   for (uint32_t i = threadIdx.x; i < work; i += blockDim.x) {
     uint32_t ent = s + i / TS;
     int y = py0 + (int)(i % TS);
-    BigRec B = F.recs[F.bins[ent]];
+    BigRec B = recs[bins ? bins[ent] : ent];
     if (y < B.y0 || y > B.y1 || y > py1) continue;
     int xs = max(B.x0, px0), xe = min(B.x1, px1);
     if (xs > xe) continue;
@@ -490,23 +578,15 @@ __device__ __forceinline__ void tile_raster(const FrameParams& F, int tile, unsi
       atomicMin(svis + (y - py0) * TS + (x - px0), v);
     });
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < TS * TS; i += blockDim.x) {
-    unsigned long long v = svis[i];
-    if (v != VIS_EMPTY) {
-      int x = px0 + i % TS, y = py0 + i / TS;
-      atomicMin(F.vis + (size_t)y * F.W + x, v);
-    }
-  }
-  __syncthreads();  // svis is reused by the block's next tile
 }
 
 constexpr int kBinThreads = 256;
 
 // Screen-tile binning of the large records and their tile raster in one
 // cooperative launch (all blocks co-resident; grid-wide barriers between the
-// phases): count per tile -> exclusive scan -> scatter -> per-tile raster.
-// With no large record every block returns at once, before any barrier.
+// phases): count per tile -> exclusive scan -> scatter -> per-tile raster
+// merged into vis[].  With no large record every block returns at once,
+// before any barrier.
 __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
   extern __shared__ unsigned long long svis[];
   __shared__ uint32_t part[kBinThreads];
@@ -515,10 +595,10 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
   cg::grid_group grid = cg::this_grid();
   const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
   const int ntiles = F.tiles_x * F.tiles_y;
+  const int TS = F.tile;
   for (uint32_t i = gt; i < nrec; i += gs) {  // 1. count
-    BigRec B = F.recs[i];
     int tx0, ty0, tx1, ty1;
-    rec_tiles(F, B, tx0, ty0, tx1, ty1);
+    rec_tiles(TS, F.recs[i], tx0, ty0, tx1, ty1);
     for (int ty = ty0; ty <= ty1; ty++)
       for (int tx = tx0; tx <= tx1; tx++) atomicAdd(F.tile_count + ty * F.tiles_x + tx, 1u);
   }
@@ -549,9 +629,8 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
   }
   grid.sync();
   for (uint32_t i = gt; i < nrec; i += gs) {  // 3. scatter
-    BigRec B = F.recs[i];
     int tx0, ty0, tx1, ty1;
-    rec_tiles(F, B, tx0, ty0, tx1, ty1);
+    rec_tiles(TS, F.recs[i], tx0, ty0, tx1, ty1);
     for (int ty = ty0; ty <= ty1; ty++)
       for (int tx = tx0; tx <= tx1; tx++) {
         int t = ty * F.tiles_x + tx;
@@ -561,7 +640,23 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
       }
   }
   grid.sync();
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) tile_raster(F, tile, svis);  // 4.
+  const bool persp = F.v.persp != 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {  // 4. raster
+    uint32_t s = F.tile_start[tile], e = min(F.tile_start[tile + 1], F.bin_cap);
+    if (s >= e) continue;  // uniform across the block
+    const int tx = tile % F.tiles_x, ty = tile / F.tiles_x;
+    const int px0 = tx * TS, py0 = ty * TS;
+    const int px1 = min(px0 + TS, F.v.W) - 1, py1 = min(py0 + TS, F.v.H) - 1;
+    for (int i = threadIdx.x; i < TS * TS; i += blockDim.x) svis[i] = VIS_EMPTY;
+    __syncthreads();
+    raster_into_tile(F.recs, F.bins, s, e, TS, px0, py0, px1, py1, persp, svis);
+    __syncthreads();
+    for (int i = threadIdx.x; i < TS * TS; i += blockDim.x) {
+      unsigned long long v = svis[i];
+      if (v != VIS_EMPTY) atomicMin(F.vis + (size_t)(py0 + i / TS) * F.v.W + (px0 + i % TS), v);
+    }
+    __syncthreads();
+  }
 }
 
 // Deferred resolve + shade: one thread per pixel.
@@ -572,96 +667,17 @@ __global__ void __launch_bounds__(256) k_resolve(FrameParams F) {
   s_dec[threadIdx.x] = (float)threadIdx.x / 255.0f;
   __syncthreads();
   size_t px = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t npx = (size_t)F.W * F.H;
+  size_t npx = (size_t)F.v.W * F.v.H;
   if (px >= npx) return;
-  unsigned long long v = F.vis[px];
-  V3 value;
+  const int y = (int)(px / F.v.W), x = (int)(px - (size_t)y * F.v.W);
+  V3 value, normal;
   float depth;
   uint32_t id;
-  V3 normal_out = v3(0, 0, 1);
-  if (v == VIS_EMPTY) {
-    value = v3(F.bg[0], F.bg[1], F.bg[2]);
-    depth = 1e11f;
-    id = MR_NO_TRIANGLE;
-  } else {
-    id = (uint32_t)v;
-    const uint32_t g = id >> 1;
-    const int s = (int)(id & 1u);
-    const int r = find_base(F.tri_base, F.n_renderables, g);
-    const DevRenderable& R = F.rs[r];
-    const int t = (int)(g - R.tri_base);
-    int ip[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) ip[c] = __ldg(R.mesh.idx + 3 * t + c);
-    Vtx v3c[3];
-    corners<PRE, true>(F, R, t, ip, v3c);
-    Setup S;
-    const float zn = F.znear;
-    const bool clipped = v3c[0].pos.z > zn || v3c[1].pos.z > zn || v3c[2].pos.z > zn;
-    if (clipped) {
-      Vtx sub[2][3];
-      clip_tri<true>(zn, v3c, sub);
-      // select sub-triangle s into v3c (s is 0 or 1 and exists: it won a pixel)
-#pragma unroll
-      for (int c = 0; c < 3; c++) v3c[c] = s ? sub[1][c] : sub[0][c];
-      setup_view(F, v3c, S);
-    } else if (PRE) {
-      V2 p[3];
-      float zt[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        float4 a = F.va[R.vert_base + ip[c]];
-        p[c] = v2(a.x, a.y);
-        zt[c] = a.z;
-      }
-      setup_from(F, p, zt, S);
-    } else {
-      setup_view(F, v3c, S);
-    }
-    const int y = (int)(px / F.W), x = (int)(px - (size_t)y * F.W);
-    float e1, e2;
-    row_start(S, y, e1, e2);
-    for (int c = S.x0; c < x; c++) {
-      e1 += S.n1.x;
-      e2 += S.n2.x;
-    }
-    float k0, k1, k2;
-    depth = frag_depth(S, F.persp != 0, e1, e2, k0, k1, k2);
-    // shading, src/Renderer.cpp:271-305 (FAST_LIGHT)
-    V3 color = v3(R.diffuse[0], R.diffuse[1], R.diffuse[2]);
-    if (R.has_tex) {
-      V2 uv = add2(add2(ks2(k0, v3c[0].uv), ks2(k1, v3c[1].uv)), ks2(k2, v3c[2].uv));
-      int ti = (int)((uv.y - floorf(uv.y)) * (float)R.tex_rows);
-      int tj = (int)((uv.x - floorf(uv.x)) * (float)R.tex_cols);
-      ti = min(max(ti, 0), R.tex_rows - 1);
-      tj = min(max(tj, 0), R.tex_cols - 1);
-      size_t o = 3 * ((size_t)ti * R.tex_cols + tj);
-      if (R.tex8)
-        color = v3(s_dec[R.tex8[o]], s_dec[R.tex8[o + 1]], s_dec[R.tex8[o + 2]]);
-      else
-        color = v3(R.texf[o], R.texf[o + 1], R.texf[o + 2]);
-    }
-    value = v3(R.emissive[0], R.emissive[1], R.emissive[2]);
-    if (F.lighting) {
-      V3 position = add3(add3(ks3(k0, v3c[0].pos), ks3(k1, v3c[1].pos)), ks3(k2, v3c[2].pos));
-      V3 LD = v3(F.lightdir[0], F.lightdir[1], F.lightdir[2]);
-      V3 lightdir = F.point ? normalized3(sub3(LD, position)) : LD;
-      V3 normal = add3(add3(ks3(k0, v3c[0].nrm), ks3(k1, v3c[1].nrm)), ks3(k2, v3c[2].nrm));
-      float sdiff = maxr(0.0f, dot3(normal, lightdir)) / len3(normal) + F.ambient;
-      value = add3(value, ks3(sdiff, color));
-      if (R.shininess != 0) {
-        V3 viewDir = normalized3(position);
-        V3 lv = sub3(lightdir, viewDir);
-        float spec = powf(maxr(dot3(lv, normal), 0.0f) / (len3(lv) * len3(normal)), R.shininess);
-        value = add3(value, ks3(spec, v3(R.specular[0], R.specular[1], R.specular[2])));
-      }
-      normal_out = normal;
-    }
-  }
+  resolve_pixel<PRE>(F.v, F.g, 0, F.g.n_renderables, F.vis[px], x, y, s_dec, value, depth, id, normal);
   if (F.rgb8) {
-    F.rgb8[3 * px + 0] = (uint8_t)(int)clampr(value.x * 255.0f, 0.0f, 255.0f);
-    F.rgb8[3 * px + 1] = (uint8_t)(int)clampr(value.y * 255.0f, 0.0f, 255.0f);
-    F.rgb8[3 * px + 2] = (uint8_t)(int)clampr(value.z * 255.0f, 0.0f, 255.0f);
+    F.rgb8[3 * px + 0] = to_byte(value.x);
+    F.rgb8[3 * px + 1] = to_byte(value.y);
+    F.rgb8[3 * px + 2] = to_byte(value.z);
   }
   if (F.depth) F.depth[px] = depth;
   if (F.ids) F.ids[px] = id;
@@ -671,9 +687,175 @@ __global__ void __launch_bounds__(256) k_resolve(FrameParams F) {
     F.rgbf[3 * px + 2] = value.z;
   }
   if (F.normals) {
-    F.normals[3 * px + 0] = normal_out.x;
-    F.normals[3 * px + 1] = normal_out.y;
-    F.normals[3 * px + 2] = normal_out.z;
+    F.normals[3 * px + 0] = normal.x;
+    F.normals[3 * px + 1] = normal.y;
+    F.normals[3 * px + 2] = normal.z;
+  }
+}
+
+// ---------------------------------------------------------------- batches
+// Setup of every triangle of every scene: each sub-triangle with pixels to
+// test becomes a record (warp-compacted), counted into its scene's tiles.
+__global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+  Setup S[2];
+  int kind[2] = {0, 0};
+  unsigned n_clipped = 0, n_raster = 0;
+  uint32_t scene = 0;
+  if (g < B.g.n_tris) {
+    const DevRenderable& R = B.g.rs[find_base(B.g.tri_base, 0, B.g.n_renderables, g)];
+    scene = R.scene;
+    if (!setup_triangle<true>(B.scenes[scene].v, B.g, R, g, S, kind, n_clipped))
+      atomicOr(&B.counters->error_flags, 1u);
+    n_raster = (kind[0] != 0) + (kind[1] != 0);
+  }
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    unsigned m = __ballot_sync(0xffffffffu, kind[s] != 0);
+    if (m == 0) continue;
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(&B.counters->rec_count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (kind[s]) {
+      unsigned slot = base + __popc(m & lt);
+      if (slot < B.rec_cap) {
+        B.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
+        B.rec_scene[slot] = scene;
+        const SceneRec& SR = B.scenes[scene];
+        int tx0 = S[s].x0 / B.tile, tx1 = S[s].x1 / B.tile, ty0 = S[s].y0 / B.tile, ty1 = S[s].y1 / B.tile;
+        for (int ty = ty0; ty <= ty1; ty++)
+          for (int tx = tx0; tx <= tx1; tx++)
+            atomicAdd(B.tile_count + SR.tile_base + ty * SR.tiles_x + tx, 1u);
+      }
+    }
+  }
+  warp_add(&B.counters->rasterised, n_raster);
+  warp_add(&B.counters->clipped, n_clipped);
+}
+
+// The batch's persistent kernel (cooperative launch, grid-wide barriers):
+//   1. exclusive scan of the per-tile counts (per-block segments + one block
+//      scanning the block sums), 2. scatter record indices into tile lists,
+//   3. tiles of all scenes taken from a work counter: each tile's records are
+//      staged in shared memory `chunk` at a time and rasterised into a
+//      shared-memory visibility tile, then every pixel of the tile is
+//      resolved, shaded and written to its scene's outputs.
+__global__ void __launch_bounds__(256, 2) k_batch(BatchParams B, uint32_t* block_sums) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int TS = B.tile;
+  unsigned long long* svis = (unsigned long long*)smem;
+  BigRec* s_recs = (BigRec*)(smem + (size_t)TS * TS * sizeof(unsigned long long));
+  __shared__ float s_dec[256];
+  __shared__ uint32_t s_part[32];
+  __shared__ uint32_t s_tile;
+  __shared__ View s_view;
+  __shared__ int s_meta[8];
+  cg::grid_group grid = cg::this_grid();
+  const uint32_t nb = gridDim.x, nt = blockDim.x;
+  for (uint32_t i = threadIdx.x; i < 256; i += nt) s_dec[i] = (float)i / 255.0f;
+  // 1. scan: block b owns tiles [b*seg, (b+1)*seg)
+  const uint32_t seg = (B.n_tiles + nb - 1) / nb;
+  const uint32_t t0 = min(B.n_tiles, blockIdx.x * seg), t1 = min(B.n_tiles, t0 + seg);
+  {
+    uint32_t sum = 0;
+    for (uint32_t i = t0 + threadIdx.x; i < t1; i += nt) sum += B.tile_count[i];
+    sum = __reduce_add_sync(0xffffffffu, sum);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      uint32_t tot = 0;
+      for (uint32_t w = 0; w < (nt + 31) / 32; w++) tot += s_part[w];
+      block_sums[blockIdx.x] = tot;
+    }
+  }
+  grid.sync();
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    uint32_t run = 0;
+    for (uint32_t i = 0; i < nb; i++) {
+      uint32_t v = block_sums[i];
+      block_sums[i] = run;
+      run += v;
+    }
+    B.tile_start[B.n_tiles] = run;
+    B.counters->bin_needed = run;
+    B.counters->bin_entries += run;
+  }
+  grid.sync();
+  if (threadIdx.x == 0) {
+    uint32_t run = block_sums[blockIdx.x];
+    for (uint32_t i = t0; i < t1; i++) {
+      B.tile_start[i] = run;
+      run += B.tile_count[i];
+    }
+  }
+  grid.sync();
+  // 2. scatter
+  const uint32_t nrec = min(B.counters->rec_count, B.rec_cap);
+  for (uint32_t i = blockIdx.x * nt + threadIdx.x; i < nrec; i += nb * nt) {
+    const BigRec& R = B.recs[i];
+    const SceneRec& SR = B.scenes[B.rec_scene[i]];
+    int tx0 = R.x0 / TS, tx1 = R.x1 / TS, ty0 = R.y0 / TS, ty1 = R.y1 / TS;
+    for (int ty = ty0; ty <= ty1; ty++)
+      for (int tx = tx0; tx <= tx1; tx++) {
+        uint32_t t = SR.tile_base + ty * SR.tiles_x + tx;
+        uint32_t pos = B.tile_start[t] + atomicAdd(B.tile_fill + t, 1u);
+        if (pos < B.bin_cap) B.bins[pos] = i;
+        else B.counters->bin_overflow = 1;
+      }
+  }
+  grid.sync();
+  // 3. tiles
+  for (;;) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      s_tile = atomicAdd(&B.counters->work_next, 1u);
+      if (s_tile < B.n_tiles) {
+        int sc = find_base(B.scene_tile_base, 0, B.n_scenes, s_tile);
+        const SceneRec& SR = B.scenes[sc];
+        s_view = SR.v;
+        s_meta[0] = sc;
+        s_meta[1] = (int)(s_tile - SR.tile_base);
+        s_meta[2] = SR.tiles_x;
+        s_meta[3] = (int)SR.rs_begin;
+        s_meta[4] = (int)SR.rs_end;
+        s_meta[5] = (int)(2u * B.g.tri_base[SR.rs_begin]);  // ids are reported per scene
+      }
+    }
+    __syncthreads();
+    const uint32_t tile = s_tile;
+    if (tile >= B.n_tiles) break;
+    for (int i = threadIdx.x; i < TS * TS; i += nt) svis[i] = VIS_EMPTY;
+    const SceneRec& SR = B.scenes[s_meta[0]];
+    const int lt = s_meta[1], tx = lt % s_meta[2], ty = lt / s_meta[2];
+    const int px0 = tx * TS, py0 = ty * TS;
+    const int px1 = min(px0 + TS, s_view.W) - 1, py1 = min(py0 + TS, s_view.H) - 1;
+    const uint32_t s = B.tile_start[tile], e = min(B.tile_start[tile + 1], B.bin_cap);
+    const bool persp = s_view.persp != 0;
+    for (uint32_t c0 = s; c0 < e; c0 += B.chunk) {
+      const uint32_t cn = min((uint32_t)B.chunk, e - c0);
+      __syncthreads();
+      for (uint32_t i = threadIdx.x; i < cn; i += nt) s_recs[i] = B.recs[B.bins[c0 + i]];
+      __syncthreads();
+      raster_into_tile(s_recs, nullptr, 0, cn, TS, px0, py0, px1, py1, persp, svis);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < TS * TS; i += nt) {
+      const int x = px0 + i % TS, y = py0 + i / TS;
+      if (x > px1 || y > py1) continue;
+      V3 value, normal;
+      float depth;
+      uint32_t id;
+      resolve_pixel<true>(s_view, B.g, s_meta[3], s_meta[4], svis[i], x, y, s_dec, value, depth, id, normal);
+      const size_t px = (size_t)y * s_view.W + x;
+      if (SR.rgb8) {
+        SR.rgb8[3 * px + 0] = to_byte(value.x);
+        SR.rgb8[3 * px + 1] = to_byte(value.y);
+        SR.rgb8[3 * px + 2] = to_byte(value.z);
+      }
+      if (SR.depth) SR.depth[px] = depth;
+      if (SR.ids) SR.ids[px] = id == MR_NO_TRIANGLE ? id : id - (uint32_t)s_meta[5];
+    }
   }
 }
 
@@ -702,45 +884,66 @@ __global__ void k_range(int W, int H, const float* P, const float* depth, float*
 // ------------------------------------------------------------ host launchers
 static int grid_for(size_t n, int block) { return (int)((n + block - 1) / block); }
 
+static int sm_count() {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 1;
+  }
+  return sms;
+}
+
 cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st) {
   if (M.n_tri <= 0) return cudaSuccess;
   k_validate<<<grid_for((size_t)M.n_tri, 256), 256, 0, st>>>(M, bad);
   return cudaGetLastError();
 }
 
-// Launch sequence of one frame.  With F.va set, the vertex pass runs first
+static cudaError_t launch_coop(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t st) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelExC(&cfg, fn, args);
+}
+
+// Launch sequence of one frame.  With F.g.va set, the vertex pass runs first
 // and the setup/resolve kernels read its buffers.  ev (optional, 6 events)
-// brackets the stages: clear+vertex, setup, binning, tile raster, resolve.
+// brackets the stages: clear+vertex, setup, binning+tile raster, -, resolve.
 cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev) {
-  size_t npx = (size_t)F.W * F.H;
-  const bool pre = F.va != nullptr;
+  size_t npx = (size_t)F.v.W * F.v.H;
+  const bool pre = F.g.va != nullptr;
   if (ev) cudaEventRecord(ev[0], st);
   // The clear also brings vis[] into L2 (write-allocate), so the setup
   // kernel's atomics hit L2.
   int cgrid = grid_for(npx, 256);
   k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(F.vis, npx);
-  if (pre && (F.n_verts + F.n_nrms) > 0)
-    k_vertex<<<grid_for((size_t)F.n_verts + F.n_nrms, 256), 256, 0, st>>>(F);
+  if (pre && (F.g.n_verts + F.g.n_nrms) > 0)
+    k_vertex<<<grid_for((size_t)F.g.n_verts + F.g.n_nrms, 256), 256, 0, st>>>(F.g, F.v, nullptr);
   if (ev) cudaEventRecord(ev[1], st);
-  if (F.n_tris) {
-    if (pre) k_setup<true><<<grid_for(F.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(F);
-    else k_setup<false><<<grid_for(F.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(F);
+  if (F.g.n_tris) {
+    if (pre) k_setup<true><<<grid_for(F.g.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(F);
+    else k_setup<false><<<grid_for(F.g.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(F);
   }
   if (ev) cudaEventRecord(ev[2], st);
   {
-    // one cooperative launch, as many blocks as are co-resident
-    static int grid = 0;
-    size_t smem = (size_t)32 * 32 * sizeof(unsigned long long);
-    if (!grid) {
-      int dev = 0, sms = 0, per = 0;
-      cudaGetDevice(&dev);
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    static int per = 0;
+    const size_t smem = (size_t)32 * 32 * sizeof(unsigned long long);
+    if (!per) {
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bin_tile, kBinThreads, smem);
-      grid = sms * (per > 0 ? per : 1);
+      if (per <= 0) per = 1;
     }
     FrameParams Fc = F;
     void* args[] = {&Fc};
-    cudaError_t e = cudaLaunchCooperativeKernel((const void*)k_bin_tile, grid, kBinThreads, args, smem, st);
+    cudaError_t e = launch_coop((const void*)k_bin_tile, sm_count() * per, kBinThreads, args, smem, st);
     if (e != cudaSuccess) return e;
   }
   if (ev) cudaEventRecord(ev[3], st);
@@ -751,8 +954,42 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   return cudaGetLastError();
 }
 
-cudaError_t launch_range(int W, int H, const float* dP, const float* depth, float* xyz,
-                         cudaStream_t st) {
+size_t batch_smem(int tile, int chunk) {
+  return (size_t)tile * tile * sizeof(unsigned long long) + (size_t)chunk * sizeof(BigRec);
+}
+
+// Co-resident blocks of k_batch for the given shape (its cooperative grid).
+int batch_grid(int tile, int chunk, int threads) {
+  int per = 0;
+  size_t smem = batch_smem(tile, chunk);
+  cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch, threads, smem);
+  if (per <= 0) return 0;
+  return sm_count() * per;
+}
+
+// Launch sequence of a batch: vertex pass, setup + tile counts, persistent
+// fused kernel.  block_sums holds grid + 1 words.  ev (optional, 4 events)
+// brackets vertex pass, setup, fused kernel.
+cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
+                         cudaEvent_t* ev) {
+  if (ev) cudaEventRecord(ev[0], st);
+  if (B.g.n_verts + B.g.n_nrms > 0) {
+    View none = {};
+    k_vertex<<<grid_for((size_t)B.g.n_verts + B.g.n_nrms, 256), 256, 0, st>>>(B.g, none, B.scenes);
+  }
+  if (ev) cudaEventRecord(ev[1], st);
+  if (B.g.n_tris) k_setup_batch<<<grid_for(B.g.n_tris, 256), 256, 0, st>>>(B);
+  if (ev) cudaEventRecord(ev[2], st);
+  BatchParams Bc = B;
+  void* args[] = {&Bc, &block_sums};
+  cudaError_t e = launch_coop((const void*)k_batch, grid, threads, args, batch_smem(B.tile, B.chunk), st);
+  if (ev) cudaEventRecord(ev[3], st);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_range(int W, int H, const float* dP, const float* depth, float* xyz, cudaStream_t st) {
   size_t npx = (size_t)W * H;
   k_range<<<grid_for(npx, 256), 256, 0, st>>>(W, H, dP, depth, xyz);
   return cudaGetLastError();

@@ -1,7 +1,7 @@
 // Data layout shared by the host side of the C ABI and the kernels: one
-// resident mesh, one renderable of a frame, the setup record of a large
-// sub-triangle, per-frame counters and the kernel parameter block.  Plain
-// C++ (no device code), so host translation units can include it.
+// resident mesh, one renderable, the view of one frame, the setup record of a
+// rasterised sub-triangle, per-frame counters and the kernel parameter
+// blocks.  Plain C++ (no device code), so host translation units can include it.
 #pragma once
 #include <stdint.h>
 #include <vector_types.h>
@@ -29,7 +29,7 @@ struct DevMesh {
   int32_t has_uv;       // texcoords and texcoordsI both non-empty
 };
 
-// One renderable of the frame: mesh, matrices and material.
+// One renderable: mesh, matrices and material.
 struct DevRenderable {
   float mv[12];         // rows 0..2 of view * transform (src/Renderer.cpp:337)
   float nm[12];         // rows 0..2 of inverse(mv)^T (src/Renderer.cpp:338)
@@ -37,6 +37,7 @@ struct DevRenderable {
   uint32_t tri_base;    // global index of the first triangle
   uint32_t vert_base;   // global index of the first vertex in the per-frame vertex buffers
   uint32_t nrm_base;    // global index of the first normal
+  uint32_t scene;       // frame (scene) this renderable belongs to (batches)
   int32_t has_tex;      // texturing on and the material has a texture
   float diffuse[3], specular[3], emissive[3], shininess;
   const uint8_t* tex8;  // rows x cols x 3 bytes (decoded b/255), or
@@ -44,8 +45,35 @@ struct DevRenderable {
   int32_t tex_rows, tex_cols;
 };
 
-// Setup record of a sub-triangle too large for the setup kernel to
-// rasterise itself; 64 bytes, written once, read by the tile rasteriser.
+// Renderer state of one frame that the kernels read (src/Renderer.cpp:311-326).
+struct View {
+  int W, H;
+  float w, h;
+  float P[16];
+  int persp;
+  float znear;
+  float lightdir[3];
+  int point;
+  float ambient;
+  int lighting, save_normals;
+  float bg[3];
+};
+
+// Geometry of a launch: renderable table, base tables and the per-vertex
+// buffers of the vertex pass (va null: kernels transform per triangle).
+struct Geo {
+  const DevRenderable* rs;
+  const uint32_t* tri_base;   // n_renderables + 1 prefix of triangle counts
+  const uint32_t* vert_base;  // n_renderables + 1 prefix of vertex counts
+  const uint32_t* nrm_base;   // n_renderables + 1 prefix of normal counts
+  int n_renderables;
+  uint32_t n_tris, n_verts, n_nrms;
+  float4* va;                 // (pixel x, pixel y, z term, view z) per vertex
+  float2* vb;                 // (view x, view y) per vertex
+  float4* vn;                 // view-space normal per normal
+};
+
+// Setup record of a rasterised sub-triangle (64 bytes).
 struct __align__(16) BigRec {
   float p0x, p0y, p2x, p2y;   // pixel-space corners 0 and 2
   float n1x, n1y, n2x, n2y;   // edge-function gradients
@@ -57,35 +85,18 @@ struct __align__(16) BigRec {
 struct Counters {
   unsigned long long triangles, clipped, rasterised, small_direct, binned, bin_entries;
   unsigned int error_flags;
-  unsigned int rec_count;      // big records written
+  unsigned int rec_count;      // records written
   unsigned int bin_needed;     // total (tile, record) pairs requested
   unsigned int bin_overflow;
+  unsigned int work_next;      // persistent-kernel work counter
+  unsigned int pad[3];
 };
 
+// One-frame launch.
 struct FrameParams {
-  int W, H;
-  float w, h;
-  float P[16];
-  int persp;
-  float znear;
-  float lightdir[3];
-  int point;
-  float ambient;
-  int lighting, save_normals;
-  float bg[3];
-  int n_renderables;
-  uint32_t n_tris;
+  View v;
+  Geo g;
   int tile, tiles_x, tiles_y, small_max;
-  const DevRenderable* rs;
-  const uint32_t* tri_base;   // n_renderables + 1 prefix of triangle counts
-  const uint32_t* vert_base;  // n_renderables + 1 prefix of vertex counts
-  const uint32_t* nrm_base;   // n_renderables + 1 prefix of normal counts
-  uint32_t n_verts, n_nrms;
-  // Per-frame vertex buffers written by the vertex pass (null: the setup and
-  // resolve kernels transform vertices themselves, per triangle).
-  float4* va;                 // (pixel x, pixel y, z term, view z) per vertex
-  float2* vb;                 // (view x, view y) per vertex
-  float4* vn;                 // view-space normal per normal
   unsigned long long* vis;    // W*H
   BigRec* recs;
   uint32_t rec_cap;
@@ -99,6 +110,36 @@ struct FrameParams {
   float* rgbf;
   uint32_t* ids;
   float* normals;
+  Counters* counters;
+};
+
+// One scene of a batch: its view, tiles and output buffers.
+struct SceneRec {
+  View v;
+  int tiles_x, tiles_y;
+  uint32_t tile_base;         // first tile in the batch-wide tile index space
+  uint32_t rs_begin, rs_end;  // renderables of this scene
+  uint8_t* rgb8;
+  float* depth;
+  uint32_t* ids;
+};
+
+// Batched launch: many scenes, one persistent fused bin-raster-shade kernel.
+struct BatchParams {
+  Geo g;
+  const SceneRec* scenes;
+  const uint32_t* scene_tile_base;  // n_scenes + 1 prefix of tile counts
+  int n_scenes;
+  uint32_t n_tiles;
+  int tile, chunk;                  // tile edge, records staged per pass
+  BigRec* recs;
+  uint32_t rec_cap;
+  uint32_t* rec_scene;              // scene of each record
+  uint32_t* tile_count;             // n_tiles
+  uint32_t* tile_start;             // n_tiles + 1
+  uint32_t* tile_fill;              // n_tiles
+  uint32_t* bins;
+  uint32_t bin_cap;
   Counters* counters;
 };
 

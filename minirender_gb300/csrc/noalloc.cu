@@ -136,31 +136,31 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   const int tx = (W + kTile - 1) / kTile, ty = (H + kTile - 1) / kTile;
   FrameParams F;
   memset(&F, 0, sizeof(F));
-  F.W = W;
-  F.H = H;
-  F.w = (float)W;
-  F.h = (float)H;
-  memcpy(F.P, f->projection, sizeof(F.P));
+  F.v.W = W;
+  F.v.H = H;
+  F.v.w = (float)W;
+  F.v.h = (float)H;
+  memcpy(F.v.P, f->projection, sizeof(F.v.P));
   // Renderer::render, src/Renderer.cpp:317-326.
-  F.persp = f->projection[15] == 0;
-  float zn = F.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
-  F.znear = -zn;
-  F.point = f->light_is_point != 0;
-  if (F.point) affine(f->view, f->light, F.lightdir);
-  else normalized(f->light, F.lightdir);
-  F.ambient = f->ambient;
-  F.lighting = f->lighting != 0;
-  memcpy(F.bg, f->background, sizeof(F.bg));
-  F.n_renderables = 1;
-  F.n_tris = (uint32_t)M.n_tri;
+  F.v.persp = f->projection[15] == 0;
+  float zn = F.v.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
+  F.v.znear = -zn;
+  F.v.point = f->light_is_point != 0;
+  if (F.v.point) affine(f->view, f->light, F.v.lightdir);
+  else normalized(f->light, F.v.lightdir);
+  F.v.ambient = f->ambient;
+  F.v.lighting = f->lighting != 0;
+  memcpy(F.v.bg, f->background, sizeof(F.v.bg));
+  F.g.n_renderables = 1;
+  F.g.n_tris = (uint32_t)M.n_tri;
   F.tile = kTile;
   F.tiles_x = tx;
   F.tiles_y = ty;
   // Every sub-triangle is rasterised by the setup kernel itself, so no
   // (data-dependent) record or bin storage is needed.
   F.small_max = 0x7fffffff;
-  F.rs = (const DevRenderable*)(S + kRsOff);
-  F.tri_base = (const uint32_t*)(S + kBaseOff);
+  F.g.rs = (const DevRenderable*)(S + kRsOff);
+  F.g.tri_base = (const uint32_t*)(S + kBaseOff);
   F.vis = (unsigned long long*)(S + kVisOff);
   F.recs = nullptr;
   F.rec_cap = 0;

@@ -1,0 +1,89 @@
+"""Batched rendering (mr_render_batch): every scene of a batch equals the
+oracle's render of that scene alone (bit-exact ids and depth, RGB8 within
+1 LSB), with and without CUDA-graph replay, for every tuning."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import edge_scenes as E
+from parity import assert_parity, compare
+from minirender_gb300 import projection as pj
+from minirender_gb300 import workloads as W
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+REPORT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
+
+
+def _items():
+    items = [W.config4_scene(s) for s in range(6)]
+    items.append(W.config1())
+    items.append(W.config2(level=6, width=480, height=270, tex_size=256))
+    for name in ("near_clip", "ortho_negative_z", "ties", "big_triangles", "texture_wrap"):
+        items.append(E.ALL[name]())
+    return items
+
+
+@pytest.fixture(scope="module")
+def batch(product_lib):
+    from minirender_gb300.batch import BatchRenderer
+    b = BatchRenderer(0)
+    yield b
+    b.close()
+
+
+@pytest.fixture(scope="module")
+def refs():
+    return [O.render(st, sc) for st, sc in _items()]
+
+
+def _check_all(b, items, refs, tag):
+    b.render(items)
+    out = []
+    for i, ref in enumerate(refs):
+        got = b.read(i)
+        got["image"] = ref["image"]  # the batch path outputs bytes, not floats
+        stats = compare(got, ref, f"batch_{tag}_{i}")
+        out.append(stats)
+        assert_parity(stats)
+    os.makedirs(REPORT, exist_ok=True)
+    with open(os.path.join(REPORT, "parity_batch.jsonl"), "a") as f:
+        for s in out:
+            f.write(json.dumps(s) + "\n")
+    return out
+
+
+@pytest.mark.parametrize("graphs", [False, True])
+def test_batch_matches_oracle(batch, refs, graphs):
+    batch.ctx.set_batch_graphs(graphs)
+    batch.ctx.set_batch_tuning(16, 256, 64)
+    _check_all(batch, _items(), refs, f"g{int(graphs)}")
+
+
+def test_graph_replay_with_new_cameras(batch, refs):
+    """A second batch of the same shape replays the captured graph; new
+    cameras and lights must be picked up."""
+    batch.ctx.set_batch_graphs(True)
+    batch.ctx.set_batch_tuning(16, 256, 64)
+    items = _items()
+    _check_all(batch, items, refs, "first")
+    moved = []
+    for st, sc in items:
+        st.view = pj.mat_mul(st.view, pj.rotate_z(0.3))
+        st.light = np.array([0.5, -0.2, 1.0], np.float32)
+        moved.append((st, sc))
+    new_refs = [O.render(st, sc) for st, sc in moved]
+    _check_all(batch, moved, new_refs, "replay")
+
+
+@pytest.mark.parametrize("tile,threads,chunk", [(8, 64, 16), (16, 128, 256), (32, 256, 32), (32, 128, 128)])
+def test_batch_tuning_same_result(batch, refs, tile, threads, chunk):
+    batch.ctx.set_batch_graphs(True)
+    batch.ctx.set_batch_tuning(tile, threads, chunk)
+    try:
+        _check_all(batch, _items(), refs, f"t{tile}_{threads}_{chunk}")
+    finally:
+        batch.ctx.set_batch_tuning(16, 256, 64)
