@@ -1,0 +1,96 @@
+"""Autotuner for the batched launch: picks the screen-tile edge, the threads
+per tile block and the number of records staged per shared-memory pass of
+the persistent fused kernel by timing every candidate on the caller's own
+batch (device time of the vertex, setup and fused stages, CUDA-graph replay),
+and caches the winner in a JSON file keyed by GPU name and a coarse class of
+the batch (scene count, triangle count and pixel count, each bucketed by
+powers of two).
+
+Every candidate produces the same pixels; only the work split changes."""
+from __future__ import annotations
+
+import json
+import math
+import os
+from typing import Dict, List, Optional, Sequence, Tuple
+
+from . import capi
+
+CANDIDATES: List[Tuple[int, int, int]] = [(t, th, ch) for t in (8, 16, 32) for th in (64, 128, 256)
+                                          for ch in (32, 64, 128)]
+
+
+def cache_path() -> str:
+    return os.environ.get("MR_AUTOTUNE_CACHE",
+                          os.path.join(os.path.expanduser("~"), ".cache", "minirender_gb300", "autotune.json"))
+
+
+def gpu_name() -> str:
+    try:
+        import torch
+        return torch.cuda.get_device_name(0)
+    except Exception:
+        return "unknown-gpu"
+
+
+def batch_class(n_scenes: int, n_tris: int, n_pixels: int) -> str:
+    b = lambda x: int(math.log2(max(1, x)))  # noqa: E731
+    return f"{gpu_name()}|scenes2^{b(n_scenes)}|tris2^{b(n_tris)}|px2^{b(n_pixels)}"
+
+
+def _load(path: str) -> Dict:
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _time_candidate(ctx: capi.Context, prepared, cand, repeats: int) -> float:
+    scenes, ns, rs, nr = prepared
+    ctx.set_batch_tuning(*cand)
+    ctx.render_batch(scenes, ns, rs, nr)   # captures this shape's graph
+    ctx.batch_stats()
+    best = float("inf")
+    for _ in range(repeats):
+        ctx.render_batch(scenes, ns, rs, nr)
+        s = ctx.batch_stats()
+        best = min(best, float(s.stage_ms[3]))  # whole batch, device time
+    return best
+
+
+def tune(ctx: capi.Context, prepared, key: str, candidates: Sequence[Tuple[int, int, int]] = CANDIDATES,
+         repeats: int = 3, path: Optional[str] = None, force: bool = False) -> Dict:
+    """Times `candidates` on the prepared batch, applies and caches the best.
+    Returns {"tile", "threads", "chunk", "ms", "table"}."""
+    path = path or cache_path()
+    cache = _load(path)
+    if not force and key in cache:
+        best = cache[key]
+        ctx.set_batch_tuning(best["tile"], best["threads"], best["chunk"])
+        return best
+    ctx.set_batch_graphs(True)
+    ctx.set_profiling(True)
+    table = []
+    try:
+        for cand in candidates:
+            try:
+                ms = _time_candidate(ctx, prepared, cand, repeats)
+            except capi.MRError:
+                continue  # shape does not fit (shared memory / registers)
+            table.append({"tile": cand[0], "threads": cand[1], "chunk": cand[2], "ms": round(ms, 4)})
+    finally:
+        ctx.set_profiling(False)
+    if not table:
+        raise RuntimeError("no batch tuning candidate could run")
+    best = dict(min(table, key=lambda r: r["ms"]))
+    best["table"] = table
+    ctx.set_batch_tuning(best["tile"], best["threads"], best["chunk"])
+    cache[key] = best
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        with open(path, "w") as f:
+            json.dump(cache, f, indent=1)
+    except OSError:
+        pass
+    return best

@@ -23,14 +23,15 @@ class BatchRenderer:
         self.outputs = abi.MR_OUT_DEFAULT
 
     def _mesh_handle(self, mesh: sc.TriMesh) -> int:
-        rec = self._meshes.get(id(mesh))
-        if rec is not None and rec[2] is mesh:
+        key = sc.geometry_key(mesh)
+        rec = self._meshes.get(key)
+        if rec is not None and rec[2] is mesh.vertices:
             if rec[1] != mesh.version:
                 self.ctx.update_mesh(rec[0], mesh.desc())
-                self._meshes[id(mesh)] = (rec[0], mesh.version, mesh)
+                self._meshes[key] = (rec[0], mesh.version, mesh.vertices)
             return rec[0]
         h = self.ctx.upload_mesh(mesh.desc())
-        self._meshes[id(mesh)] = (h, mesh.version, mesh)
+        self._meshes[key] = (h, mesh.version, mesh.vertices)
         return h
 
     def _texture_handle(self, tex: np.ndarray) -> int:

@@ -790,7 +790,9 @@ static int enqueue_batch(mr_ctx* c, cudaStream_t st) {
   CK(cudaMemcpyAsync(B.scenes.p, B.h_scenes, sizeof(SceneRec) * S, cudaMemcpyHostToDevice, st), "scene upload");
   CK(cudaMemsetAsync(B.d_cnt, 0, sizeof(Counters), st), "counter reset");
   CK(cudaMemsetAsync(B.tiles.p, 0, sizeof(uint32_t) * (3 * (size_t)B.P.n_tiles + 1), st), "tile reset");
-  CK(launch_batch(B.P, B.threads, B.grid, B.block_sums.p, st, c->profiling ? c->ev : nullptr), "batch launch");
+  // stage events only outside graphs (inside a capture they would become graph nodes)
+  CK(launch_batch(B.P, B.threads, B.grid, B.block_sums.p, st, c->profiling && !B.graphs ? c->ev : nullptr),
+     "batch launch");
   return MR_OK;
 }
 
@@ -811,7 +813,12 @@ static int run_batch(mr_ctx* c) {
                   ((uint64_t)(uintptr_t)B.h_scenes[s].ids << 2));
   }
   cudaStream_t st = c->stream;
-  if (!B.graphs) return enqueue_batch(c, st);
+  if (!B.graphs) {
+    if (c->profiling) CK(cudaEventRecord(c->ev[6], st), "profiling event");
+    int rc = enqueue_batch(c, st);
+    if (c->profiling) CK(cudaEventRecord(c->ev[7], st), "profiling event");
+    return rc;
+  }
   if (!B.exec || key != B.key) {
     if (B.exec) cudaGraphExecDestroy(B.exec);
     if (B.graph) cudaGraphDestroy(B.graph);
@@ -831,7 +838,9 @@ static int run_batch(mr_ctx* c) {
     CK(cudaGraphInstantiate(&B.exec, g, 0), "graph instantiate");
     B.key = key;
   }
+  if (c->profiling) CK(cudaEventRecord(c->ev[6], st), "profiling event");
   CK(cudaGraphLaunch(B.exec, st), "graph launch");
+  if (c->profiling) CK(cudaEventRecord(c->ev[7], st), "profiling event");
   return MR_OK;
 }
 
@@ -1077,8 +1086,12 @@ MR_API int mr_get_batch_stats(mr_ctx* c, mr_stats* s) {
   s->bin_entries = (int64_t)k.bin_needed;
   s->error_flags = k.error_flags;
   if (c->profiling) {
-    s->n_stages = 3;
-    for (int i = 0; i < 3; i++) cudaEventElapsedTime(&s->stage_ms[i], c->ev[i], c->ev[i + 1]);
+    // stage_ms[0..2]: vertex pass, setup, fused kernel (launches without a
+    // graph only); stage_ms[3]: the whole batch on the device
+    s->n_stages = 4;
+    if (!c->b.graphs)
+      for (int i = 0; i < 3; i++) cudaEventElapsedTime(&s->stage_ms[i], c->ev[i], c->ev[i + 1]);
+    cudaEventElapsedTime(&s->stage_ms[3], c->ev[6], c->ev[7]);
   }
   return rc;
 }

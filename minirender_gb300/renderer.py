@@ -25,7 +25,7 @@ class Renderer:
         self.state = FrameState()
         self.scene: Optional[sc.SceneNode] = None
         self._material = None
-        self._meshes: Dict[int, tuple] = {}     # id(TriMesh) -> (handle, version, mesh)
+        self._meshes: Dict[tuple, tuple] = {}   # geometry key -> (handle, version, vertices)
         self._textures: Dict[int, tuple] = {}   # id(array) -> (handle, array)
         self._out: Optional[dict] = None
         self._rendered = False
@@ -77,15 +77,16 @@ class Renderer:
 
     # ---- frame
     def _mesh_handle(self, mesh: sc.TriMesh) -> int:
-        rec = self._meshes.get(id(mesh))
-        if rec is not None and rec[2] is mesh:
+        key = sc.geometry_key(mesh)
+        rec = self._meshes.get(key)
+        if rec is not None and rec[2] is mesh.vertices:
             h, ver, _ = rec
             if ver != mesh.version:
                 self.ctx.update_mesh(h, mesh.desc())
-                self._meshes[id(mesh)] = (h, mesh.version, mesh)
+                self._meshes[key] = (h, mesh.version, mesh.vertices)
             return h
         h = self.ctx.upload_mesh(mesh.desc())
-        self._meshes[id(mesh)] = (h, mesh.version, mesh)
+        self._meshes[key] = (h, mesh.version, mesh.vertices)
         return h
 
     def _texture_handle(self, tex: np.ndarray) -> int:

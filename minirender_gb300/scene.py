@@ -151,6 +151,13 @@ def flatten(scene: SceneNode) -> Flat:
     return Flat(nodes, meshes, textures)
 
 
+def geometry_key(mesh: TriMesh) -> tuple:
+    """Identity of a mesh's arrays: TriMesh nodes that share their arrays share
+    one resident copy on the device."""
+    return (id(mesh.vertices), id(mesh.normals), id(mesh.texcoords), id(mesh.indices),
+            id(mesh.normalsI), id(mesh.texcoordsI))
+
+
 def mesh_descs(meshes: List[TriMesh]):
     arr = (abi.mr_mesh_desc * max(1, len(meshes)))()
     for i, m in enumerate(meshes):

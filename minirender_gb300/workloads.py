@@ -379,6 +379,24 @@ def _random_rotation(rng) -> np.ndarray:
                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
 
 
+_PRIM_CACHE = {}
+
+
+def _primitive(kind: int, seg: int) -> TriMesh:
+    """A TriMesh node sharing the (read-only) arrays of one cached primitive."""
+    key = (kind, seg if kind else 0)
+    if key not in _PRIM_CACHE:
+        if kind == 0:
+            _PRIM_CACHE[key] = create_cube(1.0)
+        elif kind == 1:
+            _PRIM_CACHE[key] = create_sphere(0.6, max(2, seg // 2), seg)
+        else:
+            _PRIM_CACHE[key] = create_cylinder(0.5, 1.2, seg)
+    g = _PRIM_CACHE[key]
+    return TriMesh(g.vertices, g.normals, g.indices, normalsI=g.normalsI, texcoords=g.texcoords,
+                   texcoordsI=g.texcoordsI if g.texcoordsI.size else None)
+
+
 def config4_scene(seed: int, n_prims: int = 64, resolution=None) -> Tuple[FrameState, Scene]:
     """One batched-launch scene: a seeded hierarchy of primitives with random
     TRS transforms and Blinn-Phong materials, camera on a radius-12 sphere."""
@@ -388,12 +406,7 @@ def config4_scene(seed: int, n_prims: int = 64, resolution=None) -> Tuple[FrameS
     for k in range(n_prims):
         kind = int(rng.integers(0, 3))
         seg = int(rng.integers(8, 65))
-        if kind == 0:
-            mesh = create_cube(1.0)
-        elif kind == 1:
-            mesh = create_sphere(0.6, max(2, seg // 2), seg)
-        else:
-            mesh = create_cylinder(0.5, 1.2, seg)
+        mesh = _primitive(kind, seg)
         sc = rng.uniform(0.2, 2.0)
         m = np.eye(4)
         m[:3, :3] = _random_rotation(rng) * sc
