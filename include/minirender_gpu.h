@@ -227,6 +227,63 @@ MR_API int mr_get_batch_outputs(mr_ctx* ctx, int32_t scene, mr_outputs* out);
 /* Waits for the last batch; counters and stage times (vertex, setup, fused). */
 MR_API int mr_get_batch_stats(mr_ctx* ctx, mr_stats* out);
 
+/* ---- render server ---------------------------------------------------------
+ * No counterpart in the reference (one synchronous Renderer::render() per
+ * frame).  A worker thread keeps meshes, textures and framebuffers resident,
+ * admits queued requests against a device-memory budget and renders them in
+ * batches as they arrive: while some batches run on the device the next ones
+ * are formed and launched on other streams (continuous batching).  Each
+ * request renders one mesh (one renderable of Renderer::render) and its
+ * result is identical whether it ran alone or in a mix. */
+typedef struct mr_server mr_server;
+
+typedef struct mr_server_opts {
+    uint64_t budget_bytes;   /* device memory the server may commit (resident meshes + in-flight requests) */
+    int32_t slots;           /* batches in flight at once (>= 1) */
+    int32_t max_batch;       /* requests per batch (>= 1) */
+    int32_t tile, threads, chunk;   /* batch tuning, as mr_set_batch_tuning */
+} mr_server_opts;
+
+typedef struct mr_request {
+    mr_frame frame;
+    uint64_t mesh_key;        /* caller's id of the mesh; a resident key is re-rendered without upload */
+    mr_mesh_desc mesh;        /* host arrays, read when the mesh is not resident; valid until done */
+    float transform[16];      /* world transform of the mesh */
+    mr_material material;     /* material.texture is ignored: see texture_key */
+    uint64_t texture_key;     /* 0: no texture */
+    const uint8_t* texture_rgb8;   /* rows x cols x 3, read when the texture is not resident */
+    int32_t tex_rows, tex_cols;
+    int32_t outputs;          /* MR_OUT_RGB8 | MR_OUT_DEPTH | MR_OUT_TRI_ID */
+    uint8_t* rgb8;            /* host destinations (page-locked memory lets copies overlap), or NULL */
+    float* depth;
+    uint32_t* tri_id;
+} mr_request;
+
+typedef struct mr_request_info {
+    int32_t status;           /* MR_OK, or the request's error */
+    int32_t batch_size;       /* requests in the batch it ran in */
+    double queue_us;          /* submit -> launch */
+    double latency_us;        /* submit -> outputs in host memory */
+} mr_request_info;
+
+typedef struct mr_server_stats {
+    int64_t submitted, completed, rejected, batches, in_queue, in_flight;
+    double mean_batch, p50_us, p99_us, max_us, frames_per_s;
+    uint64_t resident_bytes, committed_bytes;
+} mr_server_stats;
+
+MR_API int mr_server_create(mr_ctx* ctx, const mr_server_opts* opts, mr_server** out);
+/* Queues a request; MR_E_BUDGET if it can never fit the budget. */
+MR_API int mr_server_submit(mr_server* srv, const mr_request* req, uint64_t* ticket);
+/* Waits up to timeout_us (0: poll) for a request; MR_E_NOT_READY if not done.
+ * A request is forgotten once it has been reported done. */
+MR_API int mr_server_wait(mr_server* srv, uint64_t ticket, int64_t timeout_us, mr_request_info* info);
+/* Latency percentiles over the requests completed since the last reset. */
+MR_API int mr_server_get_stats(mr_server* srv, mr_server_stats* out);
+MR_API int mr_server_reset_stats(mr_server* srv);
+/* Drains the queue, stops the worker and releases the server's memory. */
+MR_API int mr_server_destroy(mr_server* srv);
+
 /* ---- rendering without any device allocation ----------------------------
  * No counterpart in the reference (its CPU Renderer never touches device
  * memory).  For callers that must not allocate device memory themselves or

@@ -78,3 +78,28 @@ class mr_stats(C.Structure):
 
 class mr_batch_scene(C.Structure):
     _fields_ = [("frame", mr_frame), ("first_renderable", C.c_int32), ("n_renderables", C.c_int32)]
+
+
+class mr_server_opts(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("slots", C.c_int32), ("max_batch", C.c_int32),
+                ("tile", C.c_int32), ("threads", C.c_int32), ("chunk", C.c_int32)]
+
+
+class mr_request(C.Structure):
+    _fields_ = [("frame", mr_frame), ("mesh_key", C.c_uint64), ("mesh", mr_mesh_desc), ("transform", F16),
+                ("material", mr_material), ("texture_key", C.c_uint64), ("texture_rgb8", C.c_void_p),
+                ("tex_rows", C.c_int32), ("tex_cols", C.c_int32), ("outputs", C.c_int32),
+                ("rgb8", C.c_void_p), ("depth", C.c_void_p), ("tri_id", C.c_void_p)]
+
+
+class mr_request_info(C.Structure):
+    _fields_ = [("status", C.c_int32), ("batch_size", C.c_int32), ("queue_us", C.c_double),
+                ("latency_us", C.c_double)]
+
+
+class mr_server_stats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("rejected", C.c_int64),
+                ("batches", C.c_int64), ("in_queue", C.c_int64), ("in_flight", C.c_int64),
+                ("mean_batch", C.c_double), ("p50_us", C.c_double), ("p99_us", C.c_double),
+                ("max_us", C.c_double), ("frames_per_s", C.c_double), ("resident_bytes", C.c_uint64),
+                ("committed_bytes", C.c_uint64)]

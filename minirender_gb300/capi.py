@@ -50,6 +50,12 @@ _SIGS = {
     "mr_read_batch": ([_P, _I, _P, _P, _P], C.c_int),
     "mr_get_batch_outputs": ([_P, _I, C.POINTER(abi.mr_outputs)], C.c_int),
     "mr_get_batch_stats": ([_P, C.POINTER(abi.mr_stats)], C.c_int),
+    "mr_server_create": ([_P, C.POINTER(abi.mr_server_opts), C.POINTER(_P)], C.c_int),
+    "mr_server_submit": ([_P, C.POINTER(abi.mr_request), C.POINTER(C.c_uint64)], C.c_int),
+    "mr_server_wait": ([_P, C.c_uint64, C.c_int64, C.POINTER(abi.mr_request_info)], C.c_int),
+    "mr_server_get_stats": ([_P, C.POINTER(abi.mr_server_stats)], C.c_int),
+    "mr_server_reset_stats": ([_P], C.c_int),
+    "mr_server_destroy": ([_P], C.c_int),
     "mr_collect_shapes": ([_P, _I, _P, _I, C.POINTER(_I)], C.c_int),
     "mr_mat4_mul": ([_P, _P, _P], None),
     "mr_mat4_inverse": ([_P, _P], None),

@@ -7,159 +7,7 @@
 // whose size is data dependent -- the (tile, triangle) bin list -- is
 // checked on the device; an overflow is detected at the next
 // synchronisation and the frame is re-run with a larger list.
-#include <cuda_runtime.h>
-#include <stdio.h>
-#include <string.h>
-
-#include <algorithm>
-#include <mutex>
-#include <string>
-#include <vector>
-
-#include "host_math.h"
-#include "layout.h"
-
-namespace mrg {
-cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st);
-cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev);
-cudaError_t launch_range(int W, int H, const float* dP, const float* depth, float* xyz,
-                         cudaStream_t st);
-cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
-                         cudaEvent_t* ev);
-int batch_grid(int tile, int chunk, int threads);
-}  // namespace mrg
-
-using namespace mrg;
-
-namespace {
-
-struct MeshRec {
-  bool live = false;
-  void* mem = nullptr;
-  DevMesh d{};
-  int32_t n_idx = 0;
-};
-
-struct TexRec {
-  bool live = false;
-  void* mem = nullptr;
-  bool rgb8 = false;
-  int32_t rows = 0, cols = 0;
-};
-
-template <typename T>
-struct DevBuf {
-  T* p = nullptr;
-  size_t cap = 0;  // elements
-  cudaError_t ensure(size_t n) {
-    if (n <= cap && p) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t want = std::max<size_t>(n, 1);
-    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
-    if (e == cudaSuccess) cap = want;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-};
-
-size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
-}  // namespace
-
-struct mr_ctx {
-  int device = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t stream = nullptr;
-  std::recursive_mutex mu;
-  std::vector<MeshRec> meshes;
-  std::vector<TexRec> textures;
-  DevBuf<unsigned long long> vis;
-  DevBuf<uint8_t> rgb8;
-  DevBuf<float> depth, rgbf, normals, range;
-  DevBuf<uint32_t> ids;
-  DevBuf<BigRec> recs;
-  DevBuf<uint32_t> bins;
-  DevBuf<uint32_t> tiles;
-  DevBuf<DevRenderable> rs;
-  DevBuf<uint32_t> tri_base;   // tri, vertex and normal base tables, 3 x (n+1)
-  DevBuf<float4> va, vn;        // per-frame vertex-pass outputs
-  DevBuf<float2> vb;
-  DevBuf<float> dP;
-  DevRenderable* h_rs = nullptr;
-  size_t h_rs_cap = 0;
-  uint32_t* h_tri_base = nullptr;
-  Counters* d_cnt = nullptr;
-  Counters* h_cnt = nullptr;
-  cudaEvent_t ev[8] = {};
-  cudaEvent_t staged = nullptr;
-  bool profiling = false;
-  int tile = 16;
-  int small_max = 64;
-  bool have_frame = false;
-  bool pending = false;  // a frame was launched and not yet checked
-  FrameParams last{};
-  mr_frame last_frame{};
-  int outputs = 0;
-  std::string err;
-
-  // ---- batches
-  struct Batch {
-    int tile = 16, threads = 256, chunk = 64;
-    bool graphs = true;
-    DevBuf<DevRenderable> rs;
-    DevBuf<uint32_t> bases;
-    DevBuf<SceneRec> scenes;
-    DevBuf<uint32_t> stb;
-    DevBuf<float4> va, vn;
-    DevBuf<float2> vb;
-    DevBuf<BigRec> recs;
-    DevBuf<uint32_t> rec_scene, tiles, bins, block_sums;
-    DevBuf<uint8_t> out8;
-    DevBuf<float> outd;
-    DevBuf<uint32_t> outi;
-    DevRenderable* h_rs = nullptr;
-    size_t h_rs_cap = 0;
-    uint32_t* h_u32 = nullptr;  // bases (3(n+1)) then scene tile bases (S+1)
-    size_t h_u32_cap = 0;
-    SceneRec* h_scenes = nullptr;
-    size_t h_scenes_cap = 0;
-    Counters* d_cnt = nullptr;
-    Counters* h_cnt = nullptr;
-    BatchParams P{};
-    int grid = 0;
-    int n_scenes = 0, n_rs = 0;
-    std::vector<int> W, H;
-    std::vector<size_t> px_off;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    std::vector<uint64_t> key;
-    cudaEvent_t done = nullptr;
-    bool have = false;
-  } b;
-};
-
-static int fail(mr_ctx* c, int code, const std::string& msg) {
-  if (c) c->err = msg;
-  return code;
-}
-
-static int cuda_fail(mr_ctx* c, cudaError_t e, const char* what) {
-  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
-  if (e == cudaErrorMemoryAllocation) return fail(c, MR_E_NOMEM, m);
-  return fail(c, MR_E_CUDA, m);
-}
-
-#define CK(expr, what)                              \
-  do {                                              \
-    cudaError_t _e = (expr);                        \
-    if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
-  } while (0)
+#include "internal.h"
 
 extern "C" {
 
@@ -202,9 +50,7 @@ MR_API int mr_create(int device, mr_ctx** out) {
   for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming);
   if (e == cudaSuccess) e = c->dP.ensure(16);
-  if (e == cudaSuccess) e = cudaMalloc(&c->b.d_cnt, sizeof(Counters));
-  if (e == cudaSuccess) e = cudaMallocHost(&c->b.h_cnt, sizeof(Counters));
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->b.done, cudaEventDisableTiming);
+
   if (e != cudaSuccess) {
     delete c;
     return e == cudaErrorMemoryAllocation ? MR_E_NOMEM : MR_E_CUDA;
@@ -235,18 +81,7 @@ MR_API int mr_destroy(mr_ctx* c) {
     for (auto& e : c->ev)
       if (e) cudaEventDestroy(e);
     if (c->staged) cudaEventDestroy(c->staged);
-    auto& B = c->b;
-    B.rs.release(); B.bases.release(); B.scenes.release(); B.stb.release(); B.va.release(); B.vn.release();
-    B.vb.release(); B.recs.release(); B.rec_scene.release(); B.tiles.release(); B.bins.release();
-    B.block_sums.release(); B.out8.release(); B.outd.release(); B.outi.release();
-    if (B.h_rs) cudaFreeHost(B.h_rs);
-    if (B.h_u32) cudaFreeHost(B.h_u32);
-    if (B.h_scenes) cudaFreeHost(B.h_scenes);
-    if (B.d_cnt) cudaFree(B.d_cnt);
-    if (B.h_cnt) cudaFreeHost(B.h_cnt);
-    if (B.exec) cudaGraphExecDestroy(B.exec);
-    if (B.graph) cudaGraphDestroy(B.graph);
-    if (B.done) cudaEventDestroy(B.done);
+    c->b.release();
     if (c->own) cudaStreamDestroy(c->own);
   }
   delete c;
@@ -285,7 +120,7 @@ MR_API int mr_set_profiling(mr_ctx* c, int on) {
   return MR_OK;
 }
 
-static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d) {
+static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t st) {
   DevMesh& M = m.d;
   char* base = (char*)m.mem;
   size_t off = 0;
@@ -301,7 +136,6 @@ static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d) {
   M.nidx = (const int32_t*)take((size_t)4 * d->n_indices);
   M.tidx = (const int32_t*)take((size_t)4 * (M.has_uv ? d->n_indices : 0));
   M.bad = (const uint32_t*)take((size_t)4 * ((M.n_tri + 31) / 32 + 1));
-  cudaStream_t st = c->stream;
   if (d->n_vertices) CK(cudaMemcpyAsync((void*)M.pos, d->vertices, (size_t)12 * d->n_vertices, cudaMemcpyHostToDevice, st), "mesh copy");
   if (d->n_normals) CK(cudaMemcpyAsync((void*)M.nrm, d->normals, (size_t)12 * d->n_normals, cudaMemcpyHostToDevice, st), "mesh copy");
   if (M.has_uv) CK(cudaMemcpyAsync((void*)M.uv, d->texcoords, (size_t)8 * d->n_texcoords, cudaMemcpyHostToDevice, st), "mesh copy");
@@ -337,12 +171,9 @@ static size_t mesh_bytes(const mr_mesh_desc* d, bool has_uv) {
          align256((size_t)4 * (has_uv ? d->n_indices : 0)) + align256((size_t)4 * ((ntri + 31) / 32 + 1));
 }
 
-MR_API int mr_mesh_upload(mr_ctx* c, const mr_mesh_desc* d, int32_t* out) {
-  if (!c || !out) return MR_E_INVALID;
-  std::lock_guard<std::recursive_mutex> g(c->mu);
+int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes) {
   int rc = check_desc(c, d);
   if (rc) return rc;
-  cudaSetDevice(c->device);
   MeshRec m;
   m.live = true;
   m.n_idx = d->n_indices;
@@ -351,10 +182,15 @@ MR_API int mr_mesh_upload(mr_ctx* c, const mr_mesh_desc* d, int32_t* out) {
   m.d.n_nrm = d->n_normals;
   m.d.n_uv = m.d.has_uv ? d->n_texcoords : 0;
   m.d.n_tri = d->n_indices / 3;
-  CK(cudaMalloc(&m.mem, mesh_bytes(d, m.d.has_uv)), "mesh allocation");
-  rc = copy_mesh(c, m, d);
+  m.bytes = mesh_bytes(d, m.d.has_uv);
+  m.stream_ordered = stream != nullptr;
+  cudaStream_t st = stream ? stream : c->stream;
+  if (stream) CK(cudaMallocAsync(&m.mem, m.bytes, stream), "mesh allocation");
+  else CK(cudaMalloc(&m.mem, m.bytes), "mesh allocation");
+  rc = copy_mesh(c, m, d, st);
   if (rc) {
-    cudaFree(m.mem);
+    if (stream) cudaFreeAsync(m.mem, stream);
+    else cudaFree(m.mem);
     return rc;
   }
   int32_t h = -1;
@@ -367,7 +203,29 @@ MR_API int mr_mesh_upload(mr_ctx* c, const mr_mesh_desc* d, int32_t* out) {
     c->meshes[h] = m;
   }
   *out = h;
+  if (bytes) *bytes = m.bytes;
   return MR_OK;
+}
+
+int mesh_destroy(mr_ctx* c, int32_t h, cudaStream_t stream) {
+  if (h < 0 || h >= (int32_t)c->meshes.size() || !c->meshes[h].live) return fail(c, MR_E_HANDLE, "unknown mesh");
+  MeshRec& m = c->meshes[h];
+  if (stream) {
+    CK(cudaFreeAsync(m.mem, stream), "mesh free");
+  } else {
+    cudaStreamSynchronize(c->stream);
+    if (m.stream_ordered) cudaDeviceSynchronize();
+    cudaFree(m.mem);
+  }
+  m = MeshRec();
+  return MR_OK;
+}
+
+MR_API int mr_mesh_upload(mr_ctx* c, const mr_mesh_desc* d, int32_t* out) {
+  if (!c || !out) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  return mesh_create(c, d, nullptr, out, nullptr);
 }
 
 MR_API int mr_mesh_update(mr_ctx* c, int32_t h, const mr_mesh_desc* d) {
@@ -382,34 +240,33 @@ MR_API int mr_mesh_update(mr_ctx* c, int32_t h, const mr_mesh_desc* d) {
       has_uv != (m.d.has_uv != 0) || (has_uv && d->n_texcoords != m.d.n_uv))
     return fail(c, MR_E_INVALID, "mr_mesh_update needs the same element counts");
   cudaSetDevice(c->device);
-  return copy_mesh(c, m, d);
+  return copy_mesh(c, m, d, c->stream);
 }
 
 MR_API int mr_mesh_free(mr_ctx* c, int32_t h) {
   if (!c) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
-  if (h < 0 || h >= (int32_t)c->meshes.size() || !c->meshes[h].live) return fail(c, MR_E_HANDLE, "unknown mesh");
   cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
-  cudaFree(c->meshes[h].mem);
-  c->meshes[h] = MeshRec();
-  return MR_OK;
+  return mesh_destroy(c, h, nullptr);
 }
 
-static int tex_upload(mr_ctx* c, const void* data, size_t bytes, bool rgb8, int32_t rows, int32_t cols,
-                      int32_t* out) {
-  if (!c || !out || !data || rows <= 0 || cols <= 0) return fail(c, MR_E_INVALID, "bad texture");
-  std::lock_guard<std::recursive_mutex> g(c->mu);
-  cudaSetDevice(c->device);
+int texture_create(mr_ctx* c, const void* data, bool rgb8, int32_t rows, int32_t cols, cudaStream_t stream,
+                   int32_t* out) {
+  if (!out || !data || rows <= 0 || cols <= 0) return fail(c, MR_E_INVALID, "bad texture");
   TexRec t;
   t.live = true;
   t.rgb8 = rgb8;
   t.rows = rows;
   t.cols = cols;
-  CK(cudaMalloc(&t.mem, bytes), "texture allocation");
-  cudaError_t e = cudaMemcpyAsync(t.mem, data, bytes, cudaMemcpyHostToDevice, c->stream);
+  t.bytes = (size_t)rows * cols * (rgb8 ? 3 : 12);
+  t.stream_ordered = stream != nullptr;
+  cudaStream_t st = stream ? stream : c->stream;
+  if (stream) CK(cudaMallocAsync(&t.mem, t.bytes, stream), "texture allocation");
+  else CK(cudaMalloc(&t.mem, t.bytes), "texture allocation");
+  cudaError_t e = cudaMemcpyAsync(t.mem, data, t.bytes, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) {
-    cudaFree(t.mem);
+    if (stream) cudaFreeAsync(t.mem, stream);
+    else cudaFree(t.mem);
     return cuda_fail(c, e, "texture copy");
   }
   int32_t h = -1;
@@ -423,6 +280,29 @@ static int tex_upload(mr_ctx* c, const void* data, size_t bytes, bool rgb8, int3
   }
   *out = h;
   return MR_OK;
+}
+
+int texture_destroy(mr_ctx* c, int32_t h, cudaStream_t stream) {
+  if (h < 0 || h >= (int32_t)c->textures.size() || !c->textures[h].live) return fail(c, MR_E_HANDLE, "unknown texture");
+  TexRec& t = c->textures[h];
+  if (stream) {
+    CK(cudaFreeAsync(t.mem, stream), "texture free");
+  } else {
+    cudaStreamSynchronize(c->stream);
+    if (t.stream_ordered) cudaDeviceSynchronize();
+    cudaFree(t.mem);
+  }
+  t = TexRec();
+  return MR_OK;
+}
+
+static int tex_upload(mr_ctx* c, const void* data, size_t bytes, bool rgb8, int32_t rows, int32_t cols,
+                      int32_t* out) {
+  (void)bytes;
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  return texture_create(c, data, rgb8, rows, cols, nullptr, out);
 }
 
 MR_API int mr_texture_upload_rgb8(mr_ctx* c, const uint8_t* rgb, int32_t rows, int32_t cols, int32_t* out) {
@@ -447,12 +327,8 @@ MR_API int mr_texture_update(mr_ctx* c, int32_t h, const void* texels) {
 MR_API int mr_texture_free(mr_ctx* c, int32_t h) {
   if (!c) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
-  if (h < 0 || h >= (int32_t)c->textures.size() || !c->textures[h].live) return fail(c, MR_E_HANDLE, "unknown texture");
   cudaSetDevice(c->device);
-  cudaStreamSynchronize(c->stream);
-  cudaFree(c->textures[h].mem);
-  c->textures[h] = TexRec();
-  return MR_OK;
+  return texture_destroy(c, h, nullptr);
 }
 
 // Launches the kernels of c->last after resetting the per-frame counters.
@@ -780,9 +656,8 @@ MR_API int mr_set_batch_graphs(mr_ctx* c, int graphs) {
   return MR_OK;
 }
 
-// Enqueues the batch described by c->b (staging already filled).
-static int enqueue_batch(mr_ctx* c, cudaStream_t st) {
-  auto& B = c->b;
+// Enqueues the batch of slot B (staging already filled) on stream st.
+static int enqueue_batch(mr_ctx* c, BatchSlot& B, cudaStream_t st, cudaEvent_t* ev) {
   const int n = B.n_rs, S = B.n_scenes;
   CK(cudaMemcpyAsync(B.rs.p, B.h_rs, sizeof(DevRenderable) * n, cudaMemcpyHostToDevice, st), "renderable upload");
   CK(cudaMemcpyAsync(B.bases.p, B.h_u32, sizeof(uint32_t) * (3 * (n + 1) + S + 1), cudaMemcpyHostToDevice, st),
@@ -790,17 +665,16 @@ static int enqueue_batch(mr_ctx* c, cudaStream_t st) {
   CK(cudaMemcpyAsync(B.scenes.p, B.h_scenes, sizeof(SceneRec) * S, cudaMemcpyHostToDevice, st), "scene upload");
   CK(cudaMemsetAsync(B.d_cnt, 0, sizeof(Counters), st), "counter reset");
   CK(cudaMemsetAsync(B.tiles.p, 0, sizeof(uint32_t) * (3 * (size_t)B.P.n_tiles + 1), st), "tile reset");
-  // stage events only outside graphs (inside a capture they would become graph nodes)
-  CK(launch_batch(B.P, B.threads, B.grid, B.block_sums.p, st, c->profiling && !B.graphs ? c->ev : nullptr),
-     "batch launch");
+  CK(launch_batch(B.P, B.threads, B.grid, B.block_sums.p, st, ev), "batch launch");
   return MR_OK;
 }
 
-static int run_batch(mr_ctx* c) {
-  auto& B = c->b;
+// Runs the staged batch of slot B on st; with profiling, ev[6]/ev[7] bracket
+// the whole batch and (outside graphs) ev[0..3] its stages.
+int batch_run(mr_ctx* c, BatchSlot& B, cudaStream_t st, bool profiling, cudaEvent_t* ev) {
   std::vector<uint64_t> key = {(uint64_t)B.n_scenes, (uint64_t)B.n_rs, B.P.g.n_tris, B.P.g.n_verts, B.P.g.n_nrms,
                                (uint64_t)B.tile, (uint64_t)B.threads, (uint64_t)B.chunk, (uint64_t)B.grid,
-                               (uint64_t)c->profiling, (uint64_t)(uintptr_t)c->stream,
+                               (uint64_t)profiling, (uint64_t)(uintptr_t)st,
                                (uint64_t)(uintptr_t)B.h_rs, (uint64_t)(uintptr_t)B.h_u32,
                                (uint64_t)(uintptr_t)B.h_scenes, (uint64_t)(uintptr_t)B.rs.p,
                                (uint64_t)(uintptr_t)B.bases.p, (uint64_t)(uintptr_t)B.scenes.p,
@@ -812,11 +686,10 @@ static int run_batch(mr_ctx* c) {
     key.push_back((uint64_t)(uintptr_t)B.h_scenes[s].rgb8 ^ ((uint64_t)(uintptr_t)B.h_scenes[s].depth << 1) ^
                   ((uint64_t)(uintptr_t)B.h_scenes[s].ids << 2));
   }
-  cudaStream_t st = c->stream;
   if (!B.graphs) {
-    if (c->profiling) CK(cudaEventRecord(c->ev[6], st), "profiling event");
-    int rc = enqueue_batch(c, st);
-    if (c->profiling) CK(cudaEventRecord(c->ev[7], st), "profiling event");
+    if (profiling) CK(cudaEventRecord(ev[6], st), "profiling event");
+    int rc = enqueue_batch(c, B, st, profiling ? ev : nullptr);
+    if (profiling) CK(cudaEventRecord(ev[7], st), "profiling event");
     return rc;
   }
   if (!B.exec || key != B.key) {
@@ -826,7 +699,8 @@ static int run_batch(mr_ctx* c) {
     B.graph = nullptr;
     B.key.clear();
     CK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal), "begin capture");
-    int rc = enqueue_batch(c, st);
+    // stage events only outside graphs (inside a capture they would become graph nodes)
+    int rc = enqueue_batch(c, B, st, nullptr);
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamEndCapture(st, &g);
     if (rc) {
@@ -838,20 +712,38 @@ static int run_batch(mr_ctx* c) {
     CK(cudaGraphInstantiate(&B.exec, g, 0), "graph instantiate");
     B.key = key;
   }
-  if (c->profiling) CK(cudaEventRecord(c->ev[6], st), "profiling event");
+  if (profiling) CK(cudaEventRecord(ev[6], st), "profiling event");
   CK(cudaGraphLaunch(B.exec, st), "graph launch");
-  if (c->profiling) CK(cudaEventRecord(c->ev[7], st), "profiling event");
+  if (profiling) CK(cudaEventRecord(ev[7], st), "profiling event");
   return MR_OK;
 }
 
-MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes, const mr_renderable* rs,
-                           int32_t n_rs, int32_t outputs) {
-  if (!c) return MR_E_INVALID;
-  std::lock_guard<std::recursive_mutex> g(c->mu);
+void BatchSlot::release() {
+  rs.release(); bases.release(); scenes.release(); stb.release(); va.release(); vn.release();
+  vb.release(); recs.release(); rec_scene.release(); tiles.release(); bins.release();
+  block_sums.release(); out8.release(); outd.release(); outi.release();
+  if (h_rs) cudaFreeHost(h_rs);
+  if (h_u32) cudaFreeHost(h_u32);
+  if (h_scenes) cudaFreeHost(h_scenes);
+  if (d_cnt) cudaFree(d_cnt);
+  if (h_cnt) cudaFreeHost(h_cnt);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (done) cudaEventDestroy(done);
+  for (auto& e : ev)
+    if (e) cudaEventDestroy(e);
+  h_rs = nullptr; h_u32 = nullptr; h_scenes = nullptr; d_cnt = nullptr; h_cnt = nullptr;
+  exec = nullptr; graph = nullptr; done = nullptr;
+  for (auto& e : ev) e = nullptr;
+}
+
+// Validates a batch and fills slot B's staging, buffers and launch parameters.
+int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_scenes, const mr_renderable* rs,
+                int32_t n_rs, int32_t outputs) {
   if (!sc || n_scenes <= 0 || n_rs < 0 || (n_rs > 0 && !rs)) return fail(c, MR_E_INVALID, "bad batch");
-  auto& B = c->b;
-  cudaSetDevice(c->device);
-  // validate scenes and renderable ranges
+  if (!B.d_cnt) CK(cudaMalloc(&B.d_cnt, sizeof(Counters)), "batch counters");
+  if (!B.h_cnt) CK(cudaMallocHost(&B.h_cnt, sizeof(Counters)), "batch counters");
+  if (!B.done) CK(cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming), "batch event");
   uint64_t tris = 0, verts = 0, nrms = 0, pixels = 0, tiles = 0;
   const int TS = B.tile;
   for (int32_t s = 0; s < n_scenes; s++) {
@@ -882,7 +774,7 @@ MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes
   if (tris >= ((uint64_t)1 << 31) || verts >= ((uint64_t)1 << 32) || nrms >= ((uint64_t)1 << 32) ||
       tiles >= ((uint64_t)1 << 31))
     return fail(c, MR_E_INVALID, "batch too large for 32-bit indices");
-  // staging (wait until the previous batch has consumed it)
+  // staging (wait until the previous batch of this slot has consumed it)
   CK(cudaEventSynchronize(B.done), "staging wait");
   CK(pinned(B.h_rs, B.h_rs_cap, (size_t)n_rs), "pinned staging");
   CK(pinned(B.h_u32, B.h_u32_cap, (size_t)3 * (n_rs + 1) + n_scenes + 1), "pinned staging");
@@ -891,7 +783,6 @@ MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes
   uint32_t* vbase = tb + (n_rs + 1);
   uint32_t* nbase = tb + 2 * (n_rs + 1);
   uint32_t* stb = tb + 3 * (n_rs + 1);
-  // outputs pool
   B.W.assign(n_scenes, 0);
   B.H.assign(n_scenes, 0);
   B.px_off.assign(n_scenes + 1, 0);
@@ -912,11 +803,11 @@ MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes
   CK(B.recs.ensure(2 * tris), "batch records");
   CK(B.rec_scene.ensure(2 * tris), "batch records");
   CK(B.tiles.ensure(3 * tiles + 1), "batch tiles");
-  if (B.bins.cap < std::max<size_t>((size_t)1 << 20, 2 * tris)) CK(B.bins.ensure(std::max<size_t>((size_t)1 << 20, 2 * tris)), "batch bins");
+  if (B.bins.cap < std::max<size_t>((size_t)1 << 20, 2 * tris))
+    CK(B.bins.ensure(std::max<size_t>((size_t)1 << 20, 2 * tris)), "batch bins");
   int grid = batch_grid(B.tile, B.chunk, B.threads);
   if (grid <= 0) return fail(c, MR_E_INVALID, "batch tuning does not fit on the device");
   CK(B.block_sums.ensure((size_t)grid + 1), "batch scan");
-  // renderables, bases and scenes
   uint32_t tri = 0, vb = 0, nb = 0, tile_base = 0;
   for (int32_t s = 0; s < n_scenes; s++) {
     const mr_frame* f = &sc[s].frame;
@@ -1004,27 +895,37 @@ MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes
   B.grid = grid;
   B.n_scenes = n_scenes;
   B.n_rs = n_rs;
-  int rc = run_batch(c);
+  return MR_OK;
+}
+
+MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes, const mr_renderable* rs,
+                           int32_t n_rs, int32_t outputs) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  BatchSlot& B = c->b;
+  int rc = batch_stage(c, B, sc, n_scenes, rs, n_rs, outputs);
+  if (rc) return rc;
+  rc = batch_run(c, B, c->stream, c->profiling, c->ev);
   if (rc) return rc;
   CK(cudaEventRecord(B.done, c->stream), "batch event");
   B.have = true;
   return MR_OK;
 }
 
-// Waits for the last batch; re-runs it while the bin list overflowed.
-static int settle_batch(mr_ctx* c) {
-  auto& B = c->b;
+// Waits for the last batch of slot B; re-runs it while the bin list overflowed.
+int batch_settle(mr_ctx* c, BatchSlot& B, cudaStream_t st) {
   if (!B.have) return fail(c, MR_E_INVALID, "no batch rendered yet");
   for (int attempt = 0; attempt < 8; attempt++) {
-    CK(cudaMemcpyAsync(B.h_cnt, B.d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "counter read");
-    CK(cudaStreamSynchronize(c->stream), "batch wait");
+    CK(cudaMemcpyAsync(B.h_cnt, B.d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, st), "counter read");
+    CK(cudaStreamSynchronize(st), "batch wait");
     if (!B.h_cnt->bin_overflow)
       return (B.h_cnt->error_flags & 1u) ? fail(c, MR_E_BAD_INDEX, "a mesh index was out of range; those triangles were skipped") : MR_OK;
     size_t want = (size_t)B.h_cnt->bin_needed + B.h_cnt->bin_needed / 4 + 1024;
     CK(B.bins.ensure(want), "batch bins");
     B.P.bins = B.bins.p;
     B.P.bin_cap = (uint32_t)std::min<size_t>(B.bins.cap, 0xFFFFFFFFu);
-    int rc = run_batch(c);
+    int rc = batch_run(c, B, st, false, nullptr);
     if (rc) return rc;
   }
   return fail(c, MR_E_NOMEM, "bin list kept overflowing");
@@ -1034,7 +935,7 @@ MR_API int mr_read_batch(mr_ctx* c, int32_t s, uint8_t* rgb8, float* depth, uint
   if (!c) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
   cudaSetDevice(c->device);
-  int rc = settle_batch(c);
+  int rc = batch_settle(c, c->b, c->stream);
   if (rc && rc != MR_E_BAD_INDEX) return rc;
   auto& B = c->b;
   if (s < 0 || s >= B.n_scenes) return fail(c, MR_E_INVALID, "scene index out of range");
@@ -1075,7 +976,7 @@ MR_API int mr_get_batch_stats(mr_ctx* c, mr_stats* s) {
   if (!c || !s) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
   cudaSetDevice(c->device);
-  int rc = settle_batch(c);
+  int rc = batch_settle(c, c->b, c->stream);
   if (rc && rc != MR_E_BAD_INDEX) return rc;
   memset(s, 0, sizeof(*s));
   const Counters& k = *c->b.h_cnt;

@@ -1,0 +1,186 @@
+// Internal declarations shared by the C-ABI translation units: the context,
+// resident meshes/textures, device buffers, batch slots and error helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "host_math.h"
+#include "layout.h"
+
+namespace mrg {
+cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st);
+cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev);
+cudaError_t launch_range(int W, int H, const float* dP, const float* depth, float* xyz,
+                         cudaStream_t st);
+cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
+                         cudaEvent_t* ev);
+int batch_grid(int tile, int chunk, int threads);
+}  // namespace mrg
+
+using namespace mrg;
+
+namespace mrgi {
+
+struct MeshRec {
+  bool live = false;
+  bool stream_ordered = false;  // allocated with cudaMallocAsync
+  void* mem = nullptr;
+  size_t bytes = 0;
+  DevMesh d{};
+  int32_t n_idx = 0;
+};
+
+struct TexRec {
+  bool live = false;
+  bool stream_ordered = false;
+  void* mem = nullptr;
+  size_t bytes = 0;
+  bool rgb8 = false;
+  int32_t rows = 0, cols = 0;
+};
+
+template <typename T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t cap = 0;  // elements
+  cudaError_t ensure(size_t n) {
+    if (n <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(n, 1);
+    cudaError_t e = cudaMalloc(&p, want * sizeof(T));
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace mrgi
+
+using namespace mrgi;
+
+// One batch in flight: its tuning, device buffers, pinned staging, counters
+// and (optionally) the CUDA graph of its launch sequence.  The context owns
+// one for mr_render_batch; a render server owns several.
+struct BatchSlot {
+  int tile = 16, threads = 256, chunk = 64;
+  bool graphs = true;
+  DevBuf<DevRenderable> rs;
+  DevBuf<uint32_t> bases;
+  DevBuf<SceneRec> scenes;
+  DevBuf<uint32_t> stb;
+  DevBuf<float4> va, vn;
+  DevBuf<float2> vb;
+  DevBuf<BigRec> recs;
+  DevBuf<uint32_t> rec_scene, tiles, bins, block_sums;
+  DevBuf<uint8_t> out8;
+  DevBuf<float> outd;
+  DevBuf<uint32_t> outi;
+  DevRenderable* h_rs = nullptr;
+  size_t h_rs_cap = 0;
+  uint32_t* h_u32 = nullptr;  // bases (3(n+1)) then scene tile bases (S+1)
+  size_t h_u32_cap = 0;
+  SceneRec* h_scenes = nullptr;
+  size_t h_scenes_cap = 0;
+  Counters* d_cnt = nullptr;
+  Counters* h_cnt = nullptr;
+  BatchParams P{};
+  int grid = 0;
+  int n_scenes = 0, n_rs = 0;
+  std::vector<int> W, H;
+  std::vector<size_t> px_off;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<uint64_t> key;
+  cudaEvent_t done = nullptr;
+  bool have = false;
+  cudaStream_t stream = nullptr;  // null: the context stream
+  cudaEvent_t ev[8] = {};         // profiling events (slots other than the context's)
+  bool profiling = false;
+  void release();
+};
+
+struct mr_ctx {
+  int device = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t stream = nullptr;
+  std::recursive_mutex mu;
+  std::vector<MeshRec> meshes;
+  std::vector<TexRec> textures;
+  DevBuf<unsigned long long> vis;
+  DevBuf<uint8_t> rgb8;
+  DevBuf<float> depth, rgbf, normals, range;
+  DevBuf<uint32_t> ids;
+  DevBuf<BigRec> recs;
+  DevBuf<uint32_t> bins;
+  DevBuf<uint32_t> tiles;
+  DevBuf<DevRenderable> rs;
+  DevBuf<uint32_t> tri_base;   // tri, vertex and normal base tables, 3 x (n+1)
+  DevBuf<float4> va, vn;        // per-frame vertex-pass outputs
+  DevBuf<float2> vb;
+  DevBuf<float> dP;
+  DevRenderable* h_rs = nullptr;
+  size_t h_rs_cap = 0;
+  uint32_t* h_tri_base = nullptr;
+  Counters* d_cnt = nullptr;
+  Counters* h_cnt = nullptr;
+  cudaEvent_t ev[8] = {};
+  cudaEvent_t staged = nullptr;
+  bool profiling = false;
+  int tile = 16;
+  int small_max = 64;
+  bool have_frame = false;
+  bool pending = false;  // a frame was launched and not yet checked
+  FrameParams last{};
+  mr_frame last_frame{};
+  int outputs = 0;
+  std::string err;
+
+  BatchSlot b;
+};
+
+inline int fail(mr_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+inline int cuda_fail(mr_ctx* c, cudaError_t e, const char* what) {
+  std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(c, MR_E_NOMEM, m);
+  return fail(c, MR_E_CUDA, m);
+}
+
+#define CK(expr, what)                              \
+  do {                                              \
+    cudaError_t _e = (expr);                        \
+    if (_e != cudaSuccess) return cuda_fail(c, _e, what); \
+  } while (0)
+
+
+extern "C" {  // internal (not exported): defined inside the C-ABI translation unit
+// Batch stages shared by mr_render_batch and the render server.
+int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_scenes, const mr_renderable* rs,
+                int32_t n_rs, int32_t outputs);
+int batch_run(mr_ctx* c, BatchSlot& B, cudaStream_t st, bool profiling, cudaEvent_t* ev);
+int batch_settle(mr_ctx* c, BatchSlot& B, cudaStream_t st);
+// Resident meshes/textures; with `stream` the memory is stream-ordered
+// (cudaMallocAsync / cudaFreeAsync) so no device-wide synchronisation occurs.
+int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes);
+int mesh_destroy(mr_ctx* c, int32_t h, cudaStream_t stream);
+int texture_create(mr_ctx* c, const void* data, bool rgb8, int32_t rows, int32_t cols, cudaStream_t stream,
+                   int32_t* out);
+int texture_destroy(mr_ctx* c, int32_t h, cudaStream_t stream);
+}  // extern "C"

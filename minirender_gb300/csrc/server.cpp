@@ -1,0 +1,467 @@
+// Render server: continuous batching of independent frame requests.
+//
+// Client threads submit requests (mr_server_submit) into a FIFO queue.  One
+// worker thread owns `slots` batch slots, each with its own CUDA stream and
+// buffers.  Whenever a slot is free it admits requests from the head of the
+// queue while the device-memory budget allows (resident meshes and textures
+// plus the estimated footprint of every request in flight), uploads meshes
+// and textures that are not resident yet (stream-ordered allocation on the
+// slot's stream), stages the batch, launches it and queues the copies of each
+// request's outputs to its host buffers -- then returns to the queue while
+// the batch runs.  Finished slots are detected with non-blocking event
+// queries; their requests are marked done with their latency.
+//
+// Meshes and textures stay resident in an LRU cache keyed by the caller's
+// ids; an entry no queued or running request refers to is evicted when the
+// budget needs room, with a stream-ordered free (no device-wide sync).
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <thread>
+#include <unordered_map>
+
+#include "internal.h"
+
+namespace {
+
+double now_us() {
+  return std::chrono::duration<double, std::micro>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+struct Request {
+  uint64_t ticket = 0;
+  mr_request req{};
+  size_t cost = 0;      // footprint while queued/running
+  size_t scene_px = 0;
+  double t_submit = 0, t_launch = 0, t_done = 0;
+  int status = 1;       // 1 queued, 2 running, 0 done
+  int result = MR_OK;
+  int batch_size = 0;
+  uint64_t mesh_key = 0, tex_key = 0;
+};
+
+struct Cached {
+  int32_t handle = -1;
+  size_t bytes = 0;
+  int refs = 0;
+  uint64_t last_use = 0;
+  cudaEvent_t ready = nullptr;  // recorded on the uploading stream after the upload
+};
+
+struct Slot {
+  BatchSlot b;
+  cudaStream_t stream = nullptr;
+  std::vector<Request*> reqs;
+  bool busy = false;
+};
+
+size_t mesh_footprint(const mr_mesh_desc& d) {
+  const size_t nt = (size_t)(d.n_indices / 3);
+  return (size_t)12 * d.n_vertices + (size_t)12 * d.n_normals + (size_t)8 * d.n_texcoords +
+         (size_t)12 * d.n_indices + nt / 8 + 4096;
+}
+
+// Device bytes a request occupies while it runs: its outputs and the
+// per-triangle, per-vertex and per-tile working buffers of a batch.
+size_t request_footprint(const mr_request& r) {
+  const size_t px = (size_t)r.frame.width * r.frame.height;
+  const size_t nt = (size_t)(r.mesh.n_indices / 3);
+  size_t out = 0;
+  if (r.outputs & MR_OUT_RGB8) out += 3 * px;
+  if (r.outputs & MR_OUT_DEPTH) out += 4 * px;
+  if (r.outputs & MR_OUT_TRI_ID) out += 4 * px;
+  return out + nt * (2 * sizeof(BigRec) + 16) + (size_t)r.mesh.n_vertices * 24 +
+         (size_t)r.mesh.n_normals * 16 + (px / 64 + 16) * 12 + sizeof(DevRenderable) + sizeof(SceneRec);
+}
+
+}  // namespace
+
+struct mr_server {
+  mr_ctx* c = nullptr;
+  mr_server_opts o{};
+  std::mutex m;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Request*> queue;
+  std::unordered_map<uint64_t, Request*> reqs;
+  std::unordered_map<uint64_t, Cached> meshes, textures;
+  size_t committed = 0, resident = 0;
+  uint64_t use_clock = 0;
+  std::vector<Slot*> slots;
+  std::thread worker;
+  bool stop = false;
+  uint64_t next_ticket = 1;
+  // statistics since the last reset
+  std::vector<double> lat;
+  int64_t submitted = 0, completed = 0, rejected = 0, batches = 0, batched = 0;
+  double t_first = 0, t_last = 0;
+
+  void run();
+  bool evict_for(size_t need, Slot* s);
+  void launch(Slot* s, std::vector<Request*>& batch);
+  void retire(Slot* s);
+};
+
+// Frees least-recently-used resident entries nobody refers to until `need`
+// more bytes fit the budget.  Called with m held.
+bool mr_server::evict_for(size_t need, Slot* s) {
+  while (committed + need > o.budget_bytes) {
+    std::unordered_map<uint64_t, Cached>* pool = nullptr;
+    uint64_t key = 0, best = ~0ull;
+    for (auto* p : {&meshes, &textures})
+      for (auto& kv : *p)
+        if (kv.second.refs == 0 && kv.second.last_use < best) {
+          best = kv.second.last_use;
+          key = kv.first;
+          pool = p;
+        }
+    if (!pool) return false;
+    Cached e = (*pool)[key];
+    pool->erase(key);
+    {
+      std::lock_guard<std::recursive_mutex> g(c->mu);
+      if (pool == &meshes) mesh_destroy(c, e.handle, s->stream);
+      else texture_destroy(c, e.handle, s->stream);
+      if (e.ready) cudaEventDestroy(e.ready);
+    }
+    committed -= e.bytes;
+    resident -= e.bytes;
+  }
+  return true;
+}
+
+// Uploads what is missing, stages and launches the batch on the slot, and
+// queues the output copies.  Called without m held (the worker owns slots).
+void mr_server::launch(Slot* s, std::vector<Request*>& batch) {
+  std::vector<mr_batch_scene> scenes(batch.size());
+  std::vector<mr_renderable> rs(batch.size());
+  int32_t outputs = 0;
+  int rc = MR_OK;
+  {
+    std::lock_guard<std::recursive_mutex> g(c->mu);
+    cudaSetDevice(c->device);
+    for (size_t i = 0; i < batch.size(); i++) {
+      Request* r = batch[i];
+      int32_t mh, th = -1;
+      cudaEvent_t mready, tready = nullptr;
+      {
+        std::lock_guard<std::mutex> lk(m);
+        mh = meshes[r->mesh_key].handle;
+        mready = meshes[r->mesh_key].ready;
+        if (r->tex_key) {
+          th = textures[r->tex_key].handle;
+          tready = textures[r->tex_key].ready;
+        }
+      }
+      // the upload may have run on another slot's stream
+      if (mready) cudaStreamWaitEvent(s->stream, mready, 0);
+      if (tready) cudaStreamWaitEvent(s->stream, tready, 0);
+      scenes[i].frame = r->req.frame;
+      scenes[i].first_renderable = (int32_t)i;
+      scenes[i].n_renderables = 1;
+      rs[i].mesh = mh;
+      rs[i].reserved = 0;
+      memcpy(rs[i].transform, r->req.transform, sizeof(rs[i].transform));
+      rs[i].material = r->req.material;
+      rs[i].material.texture = th;
+      outputs |= r->req.outputs;
+    }
+    rc = batch_stage(c, s->b, scenes.data(), (int32_t)scenes.size(), rs.data(), (int32_t)rs.size(), outputs);
+    if (rc == MR_OK) rc = batch_run(c, s->b, s->stream, false, nullptr);
+    if (rc == MR_OK) {
+      for (size_t i = 0; i < batch.size(); i++) {
+        const mr_request& q = batch[i]->req;
+        const SceneRec& SR = s->b.h_scenes[i];
+        const size_t npx = (size_t)q.frame.width * q.frame.height;
+        if (q.rgb8 && SR.rgb8) cudaMemcpyAsync(q.rgb8, SR.rgb8, 3 * npx, cudaMemcpyDeviceToHost, s->stream);
+        if (q.depth && SR.depth) cudaMemcpyAsync(q.depth, SR.depth, 4 * npx, cudaMemcpyDeviceToHost, s->stream);
+        if (q.tri_id && SR.ids) cudaMemcpyAsync(q.tri_id, SR.ids, 4 * npx, cudaMemcpyDeviceToHost, s->stream);
+      }
+      cudaMemcpyAsync(s->b.h_cnt, s->b.d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, s->stream);
+      if (cudaEventRecord(s->b.done, s->stream) != cudaSuccess) rc = MR_E_CUDA;
+      s->b.have = true;
+    }
+  }
+  std::lock_guard<std::mutex> lk(m);
+  const double t = now_us();
+  for (auto* r : batch) {
+    r->t_launch = t;
+    r->batch_size = (int)batch.size();
+    r->status = 2;
+  }
+  s->reqs = batch;
+  s->busy = true;
+  batches++;
+  batched += (int64_t)batch.size();
+  if (rc != MR_OK) {
+    for (auto* r : batch) r->result = rc;
+    cudaEventRecord(s->b.done, s->stream);
+  }
+}
+
+// Completes a slot whose event has fired.  Called with m held.
+void mr_server::retire(Slot* s) {
+  int rc = MR_OK;
+  if (s->b.h_cnt && s->b.h_cnt->bin_overflow) {
+    // rare: the batch's bin list overflowed -- re-run it at the right size
+    std::lock_guard<std::recursive_mutex> g(c->mu);
+    rc = batch_settle(c, s->b, s->stream);
+    if (rc == MR_OK || rc == MR_E_BAD_INDEX) {
+      for (size_t i = 0; i < s->reqs.size(); i++) {
+        const mr_request& q = s->reqs[i]->req;
+        const SceneRec& SR = s->b.h_scenes[i];
+        const size_t npx = (size_t)q.frame.width * q.frame.height;
+        if (q.rgb8 && SR.rgb8) cudaMemcpyAsync(q.rgb8, SR.rgb8, 3 * npx, cudaMemcpyDeviceToHost, s->stream);
+        if (q.depth && SR.depth) cudaMemcpyAsync(q.depth, SR.depth, 4 * npx, cudaMemcpyDeviceToHost, s->stream);
+        if (q.tri_id && SR.ids) cudaMemcpyAsync(q.tri_id, SR.ids, 4 * npx, cudaMemcpyDeviceToHost, s->stream);
+      }
+      cudaStreamSynchronize(s->stream);
+    }
+  } else if (s->b.h_cnt && (s->b.h_cnt->error_flags & 1u)) {
+    rc = MR_E_BAD_INDEX;
+  }
+  const double t = now_us();
+  for (auto* r : s->reqs) {
+    if (r->result == MR_OK) r->result = rc;
+    r->t_done = t;
+    r->status = 0;
+    committed -= r->cost;
+    auto it = meshes.find(r->mesh_key);
+    if (it != meshes.end()) it->second.refs--;
+    if (r->tex_key) {
+      auto jt = textures.find(r->tex_key);
+      if (jt != textures.end()) jt->second.refs--;
+    }
+    lat.push_back(r->t_done - r->t_submit);
+    completed++;
+    t_last = t;
+  }
+  s->reqs.clear();
+  s->busy = false;
+  cv_done.notify_all();
+}
+
+void mr_server::run() {
+  cudaSetDevice(c->device);
+  std::unique_lock<std::mutex> lk(m);
+  for (;;) {
+    for (Slot* s : slots)
+      if (s->busy && cudaEventQuery(s->b.done) == cudaSuccess) retire(s);
+    bool any_busy = false;
+    for (Slot* s : slots) any_busy |= s->busy;
+    if (stop && queue.empty() && !any_busy) break;
+    bool launched = false;
+    for (Slot* s : slots) {
+      if (s->busy || queue.empty()) continue;
+      std::vector<Request*> batch;
+      while (!queue.empty() && (int)batch.size() < o.max_batch) {
+        Request* r = queue.front();
+        // bytes to make resident for this request, on top of its own footprint
+        size_t extra = 0;
+        if (!meshes.count(r->mesh_key)) extra += mesh_footprint(r->req.mesh);
+        if (r->tex_key && !textures.count(r->tex_key))
+          extra += (size_t)r->req.tex_rows * r->req.tex_cols * 3;
+        if (committed + r->cost + extra > o.budget_bytes && !evict_for(r->cost + extra, s)) break;
+        queue.pop_front();
+        committed += r->cost;
+        // make the mesh / texture resident (upload is stream-ordered on this slot)
+        int rc = MR_OK;
+        if (!meshes.count(r->mesh_key)) {
+          Cached e;
+          std::lock_guard<std::recursive_mutex> g(c->mu);
+          rc = mesh_create(c, &r->req.mesh, s->stream, &e.handle, &e.bytes);
+          if (rc == MR_OK && (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
+                              cudaEventRecord(e.ready, s->stream) != cudaSuccess))
+            rc = MR_E_CUDA;
+          if (rc == MR_OK) {
+            meshes[r->mesh_key] = e;
+            committed += e.bytes;
+            resident += e.bytes;
+          }
+        }
+        if (rc == MR_OK && r->tex_key && !textures.count(r->tex_key)) {
+          Cached e;
+          e.bytes = (size_t)r->req.tex_rows * r->req.tex_cols * 3;
+          std::lock_guard<std::recursive_mutex> g(c->mu);
+          rc = texture_create(c, r->req.texture_rgb8, true, r->req.tex_rows, r->req.tex_cols, s->stream,
+                              &e.handle);
+          if (rc == MR_OK && (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
+                              cudaEventRecord(e.ready, s->stream) != cudaSuccess))
+            rc = MR_E_CUDA;
+          if (rc == MR_OK) {
+            textures[r->tex_key] = e;
+            committed += e.bytes;
+            resident += e.bytes;
+          }
+        }
+        if (rc != MR_OK) {
+          committed -= r->cost;
+          r->result = rc;
+          r->status = 0;
+          r->t_done = now_us();
+          completed++;
+          cv_done.notify_all();
+          continue;
+        }
+        meshes[r->mesh_key].refs++;
+        meshes[r->mesh_key].last_use = ++use_clock;
+        if (r->tex_key) {
+          textures[r->tex_key].refs++;
+          textures[r->tex_key].last_use = use_clock;
+        }
+        batch.push_back(r);
+      }
+      if (batch.empty()) continue;
+      lk.unlock();
+      launch(s, batch);
+      lk.lock();
+      launched = true;
+    }
+    if (!launched) cv_work.wait_for(lk, std::chrono::microseconds(50));
+  }
+}
+
+extern "C" {
+
+MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out) {
+  if (!c || !o || !out || o->slots < 1 || o->max_batch < 1 || o->budget_bytes == 0) return MR_E_INVALID;
+  mr_server* s = new mr_server();
+  s->c = c;
+  s->o = *o;
+  cudaSetDevice(c->device);
+  for (int i = 0; i < o->slots; i++) {
+    Slot* sl = new Slot();
+    sl->b.tile = o->tile ? o->tile : 16;
+    sl->b.threads = o->threads ? o->threads : 64;
+    sl->b.chunk = o->chunk ? o->chunk : 64;
+    sl->b.graphs = false;  // shapes change from batch to batch
+    if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess) {
+      delete sl;
+      for (Slot* x : s->slots) {
+        cudaStreamDestroy(x->stream);
+        delete x;
+      }
+      delete s;
+      return MR_E_CUDA;
+    }
+    s->slots.push_back(sl);
+  }
+  s->worker = std::thread([s] { s->run(); });
+  *out = s;
+  return MR_OK;
+}
+
+MR_API int mr_server_submit(mr_server* s, const mr_request* q, uint64_t* ticket) {
+  if (!s || !q || !ticket) return MR_E_INVALID;
+  if (q->frame.width <= 0 || q->frame.height <= 0 || q->mesh.n_indices % 3 || q->mesh.n_indices < 0 ||
+      (q->texture_key && (!q->texture_rgb8 || q->tex_rows <= 0 || q->tex_cols <= 0)))
+    return MR_E_INVALID;
+  Request* r = new Request();
+  r->req = *q;
+  r->mesh_key = q->mesh_key;
+  r->tex_key = q->texture_key;
+  r->cost = request_footprint(*q);
+  const size_t own = r->cost + mesh_footprint(q->mesh) + (size_t)q->tex_rows * q->tex_cols * 3;
+  std::lock_guard<std::mutex> lk(s->m);
+  if (own > s->o.budget_bytes) {
+    s->rejected++;
+    delete r;
+    return MR_E_BUDGET;
+  }
+  r->ticket = s->next_ticket++;
+  r->t_submit = now_us();
+  if (!s->submitted++) s->t_first = r->t_submit;
+  s->reqs[r->ticket] = r;
+  s->queue.push_back(r);
+  *ticket = r->ticket;
+  s->cv_work.notify_one();
+  return MR_OK;
+}
+
+MR_API int mr_server_wait(mr_server* s, uint64_t ticket, int64_t timeout_us, mr_request_info* info) {
+  if (!s) return MR_E_INVALID;
+  std::unique_lock<std::mutex> lk(s->m);
+  auto it = s->reqs.find(ticket);
+  if (it == s->reqs.end()) return MR_E_HANDLE;
+  Request* r = it->second;
+  if (r->status != 0 && timeout_us > 0)
+    s->cv_done.wait_for(lk, std::chrono::microseconds(timeout_us), [r] { return r->status == 0; });
+  if (r->status != 0) return MR_E_NOT_READY;
+  if (info) {
+    info->status = r->result;
+    info->batch_size = r->batch_size;
+    info->queue_us = r->t_launch > 0 ? r->t_launch - r->t_submit : 0;
+    info->latency_us = r->t_done - r->t_submit;
+  }
+  int rc = r->result;
+  s->reqs.erase(it);
+  delete r;
+  return rc;
+}
+
+MR_API int mr_server_get_stats(mr_server* s, mr_server_stats* o) {
+  if (!s || !o) return MR_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->m);
+  memset(o, 0, sizeof(*o));
+  o->submitted = s->submitted;
+  o->completed = s->completed;
+  o->rejected = s->rejected;
+  o->batches = s->batches;
+  o->in_queue = (int64_t)s->queue.size();
+  for (Slot* sl : s->slots) o->in_flight += sl->busy ? (int64_t)sl->reqs.size() : 0;
+  o->mean_batch = s->batches ? (double)s->batched / (double)s->batches : 0;
+  if (!s->lat.empty()) {
+    std::vector<double> v = s->lat;
+    std::sort(v.begin(), v.end());
+    auto pct = [&v](double p) { return v[std::min(v.size() - 1, (size_t)(p * (double)(v.size() - 1) + 0.5))]; };
+    o->p50_us = pct(0.50);
+    o->p99_us = pct(0.99);
+    o->max_us = v.back();
+  }
+  if (s->t_last > s->t_first) o->frames_per_s = (double)s->completed / ((s->t_last - s->t_first) * 1e-6);
+  o->resident_bytes = s->resident;
+  o->committed_bytes = s->committed;
+  return MR_OK;
+}
+
+MR_API int mr_server_reset_stats(mr_server* s) {
+  if (!s) return MR_E_INVALID;
+  std::lock_guard<std::mutex> lk(s->m);
+  s->lat.clear();
+  s->submitted = s->completed = s->rejected = s->batches = s->batched = 0;
+  s->t_first = s->t_last = 0;
+  return MR_OK;
+}
+
+MR_API int mr_server_destroy(mr_server* s) {
+  if (!s) return MR_E_INVALID;
+  {
+    std::lock_guard<std::mutex> lk(s->m);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  s->worker.join();
+  {
+    std::lock_guard<std::recursive_mutex> g(s->c->mu);
+    cudaSetDevice(s->c->device);
+    for (Slot* sl : s->slots) cudaStreamSynchronize(sl->stream);
+    for (auto& kv : s->meshes) {
+      mesh_destroy(s->c, kv.second.handle, s->slots[0]->stream);
+      if (kv.second.ready) cudaEventDestroy(kv.second.ready);
+    }
+    for (auto& kv : s->textures) {
+      texture_destroy(s->c, kv.second.handle, s->slots[0]->stream);
+      if (kv.second.ready) cudaEventDestroy(kv.second.ready);
+    }
+    for (Slot* sl : s->slots) {
+      cudaStreamSynchronize(sl->stream);
+      sl->b.release();
+      cudaStreamDestroy(sl->stream);
+      delete sl;
+    }
+  }
+  for (auto& kv : s->reqs) delete kv.second;
+  delete s;
+  return MR_OK;
+}
+
+}  // extern "C"

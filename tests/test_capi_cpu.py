@@ -47,14 +47,17 @@ def test_library_exports_every_declared_symbol(product_lib):
 def test_struct_layouts_match_ctypes(tmp_path):
     src = tmp_path / "sz.c"
     src.write_text('#include <stdio.h>\n#include "minirender_gpu.h"\n'
-                   'int main(){printf("%zu %zu %zu %zu %zu %zu %zu\\n", sizeof(mr_material), '
+                   'int main(){printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(mr_material), '
                    'sizeof(mr_mesh_desc), sizeof(mr_renderable), sizeof(mr_node), sizeof(mr_frame), '
-                   'sizeof(mr_outputs), sizeof(mr_stats));return 0;}\n')
+                   'sizeof(mr_outputs), sizeof(mr_stats), sizeof(mr_batch_scene), sizeof(mr_server_opts), '
+                   'sizeof(mr_request), sizeof(mr_request_info), sizeof(mr_server_stats));return 0;}\n')
     exe = tmp_path / "sz"
     subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
     want = [C.sizeof(t) for t in (abi.mr_material, abi.mr_mesh_desc, abi.mr_renderable, abi.mr_node,
-                                  abi.mr_frame, abi.mr_outputs, abi.mr_stats)]
+                                  abi.mr_frame, abi.mr_outputs, abi.mr_stats, abi.mr_batch_scene,
+                                  abi.mr_server_opts, abi.mr_request, abi.mr_request_info,
+                                  abi.mr_server_stats)]
     assert got == want
 
 
