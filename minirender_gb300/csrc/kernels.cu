@@ -248,9 +248,24 @@ __device__ __forceinline__ void walk_row(const Setup& S, bool persp, uint32_t id
   }
 }
 
-__device__ __forceinline__ void warp_add(unsigned long long* dst, unsigned v) {
+// Per-block statistics: warps add into shared counters, one global atomic per
+// counter and block (a single global address updated by every warp would
+// serialise in L2).  Every thread of the block must call block_flush.
+struct BlockCounters {
+  unsigned v[3];
+};
+__device__ __forceinline__ void block_count(BlockCounters& bc, int k, unsigned v) {
   unsigned s = __reduce_add_sync(0xffffffffu, v);
-  if ((threadIdx.x & 31) == 0 && s) atomicAdd(dst, (unsigned long long)s);
+  if ((threadIdx.x & 31) == 0 && s) atomicAdd(&bc.v[k], s);
+}
+__device__ __forceinline__ void block_flush(BlockCounters& bc, unsigned long long* d0, unsigned long long* d1,
+                                            unsigned long long* d2) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (bc.v[0]) atomicAdd(d0, (unsigned long long)bc.v[0]);
+    if (bc.v[1] && d1) atomicAdd(d1, (unsigned long long)bc.v[1]);
+    if (bc.v[2]) atomicAdd(d2, (unsigned long long)bc.v[2]);
+  }
 }
 
 __device__ __forceinline__ BigRec to_rec(const Setup& S, uint32_t id) {
@@ -459,6 +474,9 @@ template <bool PRE>
 __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
   __shared__ SmallRec s_rec[kSetupWarps][64];
   __shared__ int s_pre[kSetupWarps][65];
+  __shared__ BlockCounters bc;
+  if (threadIdx.x < 3) bc.v[threadIdx.x] = 0;
+  __syncthreads();
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned lt = (1u << lane) - 1u;
@@ -494,13 +512,36 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
       if (slot < F.rec_cap) F.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
     }
   }
-  // small records: stage in shared memory, then rasterise with one
-  // (triangle, row) per lane so every lane has work
+  bool direct;
+  // Small records.  When every one in the warp spans at most 4x4 pixels the
+  // lanes rasterise their own (the loops are short and nearly uniform);
+  // otherwise they are staged in shared memory and rasterised with one
+  // (triangle, row) per lane so every lane has work.
+  {
+    int span = 0;
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+      if (kind[s] == 1) span = max(span, max(S[s].x1 - S[s].x0, S[s].y1 - S[s].y0) + 1);
+    direct = __reduce_max_sync(0xffffffffu, (unsigned)span) <= 4u;
+    if (direct) {
+      unsigned long long* vis = F.vis;
+      const int W = F.v.W;
+#pragma unroll
+      for (int s = 0; s < 2; s++)
+        if (kind[s] == 1) {
+          const uint32_t id = 2u * g + (uint32_t)s;
+          for (int y = S[s].y0; y <= S[s].y1; y++)
+            walk_row(S[s], persp, id, y, S[s].x0, S[s].x1, [&](int x, unsigned long long v) {
+              atomicMin(vis + (size_t)y * W + x, v);
+            });
+        }
+    }
+  }
   int n = 0;
 #pragma unroll
   for (int s = 0; s < 2; s++) {
-    unsigned m = __ballot_sync(0xffffffffu, kind[s] == 1);
-    if (kind[s] == 1) {
+    unsigned m = __ballot_sync(0xffffffffu, kind[s] == 1 && !direct);
+    if (kind[s] == 1 && !direct) {
       SmallRec& q = s_rec[w][n + __popc(m & lt)];
       q.p0x = S[s].p0.x; q.p0y = S[s].p0.y; q.p2x = S[s].p2.x; q.p2y = S[s].p2.y;
       q.n1x = S[s].n1.x; q.n1y = S[s].n1.y; q.n2x = S[s].n2.x; q.n2y = S[s].n2.y;
@@ -549,9 +590,10 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
       }
     }
   }
-  warp_add(&F.counters->rasterised, n_raster);
-  warp_add(&F.counters->small_direct, n_small);
-  warp_add(&F.counters->clipped, n_clipped);
+  block_count(bc, 0, n_raster);
+  block_count(bc, 1, n_small);
+  block_count(bc, 2, n_clipped);
+  block_flush(bc, &F.counters->rasterised, &F.counters->small_direct, &F.counters->clipped);
 }
 
 __device__ __forceinline__ void rec_tiles(int tile, const BigRec& B, int& tx0, int& ty0, int& tx1, int& ty1) {
@@ -697,6 +739,11 @@ __global__ void __launch_bounds__(256) k_resolve(FrameParams F) {
 // Setup of every triangle of every scene: each sub-triangle with pixels to
 // test becomes a record (warp-compacted), counted into its scene's tiles.
 __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
+  __shared__ BlockCounters bc;
+  __shared__ unsigned s_fill, s_base;
+  if (threadIdx.x < 3) bc.v[threadIdx.x] = 0;
+  if (threadIdx.x == 0) s_fill = 0;
+  __syncthreads();
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
   Setup S[2];
@@ -710,13 +757,21 @@ __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
       atomicOr(&B.counters->error_flags, 1u);
     n_raster = (kind[0] != 0) + (kind[1] != 0);
   }
+  // record slots: each warp reserves within the block, the block once globally
+  unsigned m2[2], wbase = 0;
+#pragma unroll
+  for (int s = 0; s < 2; s++) m2[s] = __ballot_sync(0xffffffffu, kind[s] != 0);
+  const unsigned wn = __popc(m2[0]) + __popc(m2[1]);
+  if (lane == 0 && wn) wbase = atomicAdd(&s_fill, wn);
+  wbase = __shfl_sync(0xffffffffu, wbase, 0);
+  __syncthreads();
+  if (threadIdx.x == 0) s_base = s_fill ? atomicAdd(&B.counters->rec_count, s_fill) : 0;
+  __syncthreads();
+  unsigned base = s_base + wbase;
 #pragma unroll
   for (int s = 0; s < 2; s++) {
-    unsigned m = __ballot_sync(0xffffffffu, kind[s] != 0);
+    const unsigned m = m2[s];
     if (m == 0) continue;
-    unsigned base = 0;
-    if (lane == 0) base = atomicAdd(&B.counters->rec_count, (unsigned)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, 0);
     if (kind[s]) {
       unsigned slot = base + __popc(m & lt);
       if (slot < B.rec_cap) {
@@ -729,9 +784,11 @@ __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
             atomicAdd(B.tile_count + SR.tile_base + ty * SR.tiles_x + tx, 1u);
       }
     }
+    base += __popc(m);
   }
-  warp_add(&B.counters->rasterised, n_raster);
-  warp_add(&B.counters->clipped, n_clipped);
+  block_count(bc, 0, n_raster);
+  block_count(bc, 2, n_clipped);
+  block_flush(bc, &B.counters->rasterised, nullptr, &B.counters->clipped);
 }
 
 // The batch's persistent kernel (cooperative launch, grid-wide barriers):

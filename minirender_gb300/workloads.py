@@ -432,3 +432,47 @@ def config4_scene(seed: int, n_prims: int = 64, resolution=None) -> Tuple[FrameS
 
 def config4(n_scenes: int = 256, n_prims: int = 64):
     return [config4_scene(s, n_prims) for s in range(n_scenes)]
+
+
+# ------------------------------------------------------------------ config 5
+def config5_pool(n_meshes: int = 24, seed: int = 5, t_min: int = 1000, t_max: int = 2_000_000):
+    """Meshes for the serving stream: config-3 style soups whose triangle
+    counts are log-uniform in [t_min, t_max]; each with its palette texture."""
+    rng = np.random.default_rng(seed)
+    sizes = np.exp(rng.uniform(math.log(t_min), math.log(t_max), n_meshes)).astype(int)
+    pool = []
+    for k, n in enumerate(sizes):
+        st, sc = config3(n_tris=int(n), width=3840, height=2160, seed=seed * 1000 + k)
+        pool.append(sc.children[0])
+    return pool
+
+
+def config5_requests(pool, n: int, rate: float, seed: int = 7, rerender: float = 0.3):
+    """A Poisson request stream: arrival times (s), resolution log-uniform
+    from 128x128 to 3840x2160, a fresh mesh key (the mesh must be uploaded)
+    or, with probability `rerender`, a recently used key re-rendered from a
+    new camera."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, n))
+    out = []
+    recent: List[Tuple[int, int]] = []
+    next_key = 1
+    for i in range(n):
+        u = rng.uniform()
+        w = int(round(128 * (3840 / 128) ** u))
+        h = int(round(128 * (2160 / 128) ** u))
+        if recent and rng.uniform() < rerender:
+            key, idx = recent[int(rng.integers(0, len(recent)))]
+            angle = float(rng.uniform(-0.3, 0.3))
+        else:
+            idx = int(rng.integers(0, len(pool)))
+            key = next_key
+            next_key += 1
+            angle = 0.0
+            recent.append((key, idx))
+            recent = recent[-32:]
+        st = FrameState(width=w, height=h,
+                        projection=pj.projection_frustum(pj.deg2rad(60), f32(w) / f32(h), 0.1, 100),
+                        view=pj.rotate_z(angle), light=np.array([0.2, 0.4, 1.0], np.float32))
+        out.append({"t": float(t[i]), "state": st, "mesh": idx, "key": key})
+    return out
