@@ -51,6 +51,7 @@ def parse():
     p.add_argument("--rates", default="100,500,1000,2000,5000", help="request rates swept (config5)")
     p.add_argument("--requests", type=int, default=1500, help="requests per rate (config5)")
     p.add_argument("--scenes", type=int, default=256, help="scenes per batch (config4)")
+    p.add_argument("--tuning", default="", help="tile,threads,chunk for batches (skips the autotuner)")
     p.add_argument("--views", type=int, default=8, help="camera views per batched launch (config1-3)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs (profiling runs)")
@@ -315,7 +316,12 @@ def batch_arm(args, ws, rank, local):
     prep = br.prepare(items)
     T = sum(scene_tris(sc) for st, sc in items)
     P = sum(st.width * st.height for st, sc in items)
-    best = autotune.tune(br.ctx, prep, autotune.batch_class(len(items), T, P))
+    if args.tuning:
+        t, th, ch = (int(x) for x in args.tuning.split(","))
+        br.ctx.set_batch_tuning(t, th, ch)
+        best = {"tile": t, "threads": th, "chunk": ch, "table": None}
+    else:
+        best = autotune.tune(br.ctx, prep, autotune.batch_class(len(items), T, P))
     br.ctx.set_batch_graphs(True)
     for _ in range(max(3, args.warmup)):
         br.ctx.render_batch(*prep, br.outputs)
