@@ -51,7 +51,8 @@ def parse():
     p.add_argument("--rates", default="100,500,1000,2000,5000", help="request rates swept (config5)")
     p.add_argument("--requests", type=int, default=1500, help="requests per rate (config5)")
     p.add_argument("--scenes", type=int, default=256, help="scenes per batch (config4)")
-    p.add_argument("--tuning", default="", help="tile,threads,chunk for batches (skips the autotuner)")
+    p.add_argument("--tuning", default="",
+                   help="tile,threads,chunk or tile_w,tile_h,threads,chunk for batches (skips the autotuner)")
     p.add_argument("--views", type=int, default=8, help="camera views per batched launch (config1-3)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs (profiling runs)")
@@ -195,6 +196,7 @@ def cpu_frames_per_s(st, sc, n_threads: int, frames: int):
 
 
 STAGES = ["clear+vertex", "setup", "bin", "tile_raster", "resolve"]
+TUNING_KEYS = ("tile_w", "tile_h", "threads", "chunk")
 KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "bin": "k_bin_count+k_scan+k_bin_scatter",
            "tile_raster": "k_tile_raster", "resolve": "k_resolve"}
 
@@ -317,9 +319,11 @@ def batch_arm(args, ws, rank, local):
     T = sum(scene_tris(sc) for st, sc in items)
     P = sum(st.width * st.height for st, sc in items)
     if args.tuning:
-        t, th, ch = (int(x) for x in args.tuning.split(","))
-        br.ctx.set_batch_tuning(t, th, ch)
-        best = {"tile": t, "threads": th, "chunk": ch, "table": None}
+        tun = [int(x) for x in args.tuning.split(",")]
+        if len(tun) == 3:
+            tun = [tun[0]] + tun
+        best = {"tile_w": tun[0], "tile_h": tun[1], "threads": tun[2], "chunk": tun[3], "table": None}
+        autotune.apply(br.ctx, best)
     else:
         best = autotune.tune(br.ctx, prep, autotune.batch_class(len(items), T, P))
     br.ctx.set_batch_graphs(True)
@@ -384,7 +388,7 @@ def batch_arm(args, ws, rank, local):
                                "{256^2, 512^2, 640x480, 1280x720}, one batched launch per step",
                    "scenes": len(items), "triangles": T, "pixels": P,
                    "l2": "flushed between steps (256 MiB write); working set > L2",
-                   "tuning": {k: best[k] for k in ("tile", "threads", "chunk")}},
+                   "tuning": {k: best[k] for k in TUNING_KEYS}},
         "mtri_per_s": round(value * T / len(items) / 1e6, 2),
         "wall_value_incl_host_staging": round(len(items) * args.steps / wall, 2),
         "plain_one_frame_per_call": {"value": round(plain, 2), "wall_value": round(plain_wall, 2),
@@ -623,7 +627,7 @@ def gpu_arm(args, ws, rank, local):
         bv, best = batched_views(args, stream, flush, st, sc, args.views)
         out["batched"] = {"value": round(bv, 3), "unit": UNIT, "views_per_launch": args.views,
                           "speedup_vs_plain": round(bv / value, 3),
-                          "tuning": {k: best[k] for k in ("tile", "threads", "chunk")}}
+                          "tuning": {k: best[k] for k in TUNING_KEYS}}
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         n_threads = os.cpu_count() or 1
         frames = 2 * n_threads

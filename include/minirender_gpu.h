@@ -213,6 +213,10 @@ typedef struct mr_batch_scene {
 /* Tile edge (8/16/32), threads per tile block (64/128/256) and records
  * staged per pass in shared memory (16..256) for mr_render_batch. */
 MR_API int mr_set_batch_tuning(mr_ctx* ctx, int tile, int threads, int chunk);
+/* As mr_set_batch_tuning with a rectangular screen tile: power-of-two sides,
+ * width 4..256, height 2..32, 64..1024 pixels.  Wide tiles shorten the
+ * column-by-column edge-function replay of triangles that cross tiles. */
+MR_API int mr_set_batch_tiling(mr_ctx* ctx, int tile_w, int tile_h, int threads, int chunk);
 /* graphs != 0: the launch sequence is captured once per batch shape (scene
  * count, sizes, renderable and triangle counts, tuning) into a CUDA graph and
  * replayed; cameras, lights and materials may change between replays. */
@@ -241,7 +245,8 @@ typedef struct mr_server_opts {
     uint64_t budget_bytes;   /* device memory the server may commit (resident meshes + in-flight requests) */
     int32_t slots;           /* batches in flight at once (>= 1) */
     int32_t max_batch;       /* requests per batch (>= 1) */
-    int32_t tile, threads, chunk;   /* batch tuning, as mr_set_batch_tuning */
+    int32_t tile, threads, chunk;   /* batch tuning, as mr_set_batch_tuning (0: defaults) */
+    int32_t tile_h;          /* tile height; 0: square tiles of edge `tile` (as mr_set_batch_tiling) */
 } mr_server_opts;
 
 typedef struct mr_request {

@@ -1,10 +1,10 @@
-"""Autotuner for the batched launch: picks the screen-tile edge, the threads
-per tile block and the number of records staged per shared-memory pass of
-the persistent fused kernel by timing every candidate on the caller's own
-batch (device time of the vertex, setup and fused stages, CUDA-graph replay),
-and caches the winner in a JSON file keyed by GPU name and a coarse class of
-the batch (scene count, triangle count and pixel count, each bucketed by
-powers of two).
+"""Autotuner for the batched launch: picks the screen-tile shape (width x
+height), the threads per tile block and the number of records staged per
+shared-memory pass of the persistent fused kernel by timing every candidate
+on the caller's own batch (device time of the vertex, setup and fused
+stages, CUDA-graph replay), and caches the winner in a JSON file keyed by
+GPU name and a coarse class of the batch (scene count, triangle count and
+pixel count, each bucketed by powers of two).
 
 Every candidate produces the same pixels; only the work split changes."""
 from __future__ import annotations
@@ -16,8 +16,16 @@ from typing import Dict, List, Optional, Sequence, Tuple
 
 from . import capi
 
-CANDIDATES: List[Tuple[int, int, int]] = [(t, th, ch) for t in (8, 16, 32) for th in (64, 128, 256)
-                                          for ch in (32, 64, 128)]
+# (tile width, tile height): square tiles plus wide ones, which shorten the
+# per-row edge replay of triangles crossing several tiles.
+SHAPES: List[Tuple[int, int]] = [(8, 8), (16, 16), (32, 16), (32, 32), (64, 16), (128, 8)]
+CANDIDATES: List[Tuple[int, int, int, int]] = [(tw, th, t, ch) for tw, th in SHAPES for t in (64, 128, 256)
+                                               for ch in (32, 64, 128)]
+
+
+def apply(ctx: capi.Context, best: Dict) -> None:
+    """Sets a tuning returned by tune() (or read from its cache)."""
+    ctx.set_batch_tiling(best["tile_w"], best["tile_h"], best["threads"], best["chunk"])
 
 
 def cache_path() -> str:
@@ -48,7 +56,7 @@ def _load(path: str) -> Dict:
 
 def _time_candidate(ctx: capi.Context, prepared, cand, repeats: int) -> float:
     scenes, ns, rs, nr = prepared
-    ctx.set_batch_tuning(*cand)
+    ctx.set_batch_tiling(*cand)
     ctx.render_batch(scenes, ns, rs, nr)   # captures this shape's graph
     ctx.batch_stats()
     best = float("inf")
@@ -59,15 +67,16 @@ def _time_candidate(ctx: capi.Context, prepared, cand, repeats: int) -> float:
     return best
 
 
-def tune(ctx: capi.Context, prepared, key: str, candidates: Sequence[Tuple[int, int, int]] = CANDIDATES,
+def tune(ctx: capi.Context, prepared, key: str, candidates: Sequence[Tuple[int, int, int, int]] = CANDIDATES,
          repeats: int = 3, path: Optional[str] = None, force: bool = False) -> Dict:
-    """Times `candidates` on the prepared batch, applies and caches the best.
-    Returns {"tile", "threads", "chunk", "ms", "table"}."""
+    """Times `candidates` (tile_w, tile_h, threads, chunk) on the prepared
+    batch, applies and caches the best.
+    Returns {"tile_w", "tile_h", "threads", "chunk", "ms", "table"}."""
     path = path or cache_path()
     cache = _load(path)
-    if not force and key in cache:
+    if not force and key in cache and "tile_w" in cache[key]:
         best = cache[key]
-        ctx.set_batch_tuning(best["tile"], best["threads"], best["chunk"])
+        apply(ctx, best)
         return best
     ctx.set_batch_graphs(True)
     ctx.set_profiling(True)
@@ -78,14 +87,15 @@ def tune(ctx: capi.Context, prepared, key: str, candidates: Sequence[Tuple[int, 
                 ms = _time_candidate(ctx, prepared, cand, repeats)
             except capi.MRError:
                 continue  # shape does not fit (shared memory / registers)
-            table.append({"tile": cand[0], "threads": cand[1], "chunk": cand[2], "ms": round(ms, 4)})
+            table.append({"tile_w": cand[0], "tile_h": cand[1], "threads": cand[2], "chunk": cand[3],
+                          "ms": round(ms, 4)})
     finally:
         ctx.set_profiling(False)
     if not table:
         raise RuntimeError("no batch tuning candidate could run")
     best = dict(min(table, key=lambda r: r["ms"]))
     best["table"] = table
-    ctx.set_batch_tuning(best["tile"], best["threads"], best["chunk"])
+    apply(ctx, best)
     cache[key] = best
     try:
         os.makedirs(os.path.dirname(path), exist_ok=True)

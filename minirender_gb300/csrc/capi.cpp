@@ -637,16 +637,24 @@ static cudaError_t pinned(T*& p, size_t& cap, size_t n) {
 }
 }  // extern "C++"
 
-MR_API int mr_set_batch_tuning(mr_ctx* c, int tile, int threads, int chunk) {
+MR_API int mr_set_batch_tiling(mr_ctx* c, int tile_w, int tile_h, int threads, int chunk) {
   if (!c) return MR_E_INVALID;
-  if (tile != 8 && tile != 16 && tile != 32) return fail(c, MR_E_INVALID, "tile must be 8, 16 or 32");
+  if (!batch_tile_ok(tile_w, tile_h))
+    return fail(c, MR_E_INVALID, "tile sides must be powers of two, 4..256 x 2..32, 64..1024 pixels");
   if (threads != 64 && threads != 128 && threads != 256) return fail(c, MR_E_INVALID, "threads must be 64, 128 or 256");
   if (chunk < 16 || chunk > 256) return fail(c, MR_E_INVALID, "chunk must be in 16..256");
   std::lock_guard<std::recursive_mutex> g(c->mu);
-  c->b.tile = tile;
+  c->b.tile_w = tile_w;
+  c->b.tile_h = tile_h;
   c->b.threads = threads;
   c->b.chunk = chunk;
   return MR_OK;
+}
+
+MR_API int mr_set_batch_tuning(mr_ctx* c, int tile, int threads, int chunk) {
+  if (!c) return MR_E_INVALID;
+  if (tile != 8 && tile != 16 && tile != 32) return fail(c, MR_E_INVALID, "tile must be 8, 16 or 32");
+  return mr_set_batch_tiling(c, tile, tile, threads, chunk);
 }
 
 MR_API int mr_set_batch_graphs(mr_ctx* c, int graphs) {
@@ -673,7 +681,8 @@ static int enqueue_batch(mr_ctx* c, BatchSlot& B, cudaStream_t st, cudaEvent_t* 
 // the whole batch and (outside graphs) ev[0..3] its stages.
 int batch_run(mr_ctx* c, BatchSlot& B, cudaStream_t st, bool profiling, cudaEvent_t* ev) {
   std::vector<uint64_t> key = {(uint64_t)B.n_scenes, (uint64_t)B.n_rs, B.P.g.n_tris, B.P.g.n_verts, B.P.g.n_nrms,
-                               (uint64_t)B.tile, (uint64_t)B.threads, (uint64_t)B.chunk, (uint64_t)B.grid,
+                               (uint64_t)B.tile_w, (uint64_t)B.tile_h, (uint64_t)B.threads, (uint64_t)B.chunk,
+                               (uint64_t)B.grid,
                                (uint64_t)profiling, (uint64_t)(uintptr_t)st,
                                (uint64_t)(uintptr_t)B.h_rs, (uint64_t)(uintptr_t)B.h_u32,
                                (uint64_t)(uintptr_t)B.h_scenes, (uint64_t)(uintptr_t)B.rs.p,
@@ -745,7 +754,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   if (!B.h_cnt) CK(cudaMallocHost(&B.h_cnt, sizeof(Counters)), "batch counters");
   if (!B.done) CK(cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming), "batch event");
   uint64_t tris = 0, verts = 0, nrms = 0, pixels = 0, tiles = 0;
-  const int TS = B.tile;
+  const int TW = B.tile_w, TH = B.tile_h;
   for (int32_t s = 0; s < n_scenes; s++) {
     const mr_frame* f = &sc[s].frame;
     if (f->width <= 0 || f->height <= 0 || f->width > (1 << 16) || f->height > (1 << 16))
@@ -756,7 +765,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
         (s == 0 && sc[s].first_renderable != 0))
       return fail(c, MR_E_INVALID, "scene renderable ranges must tile the renderable array in order");
     pixels += (uint64_t)f->width * f->height;
-    tiles += (uint64_t)((f->width + TS - 1) / TS) * ((f->height + TS - 1) / TS);
+    tiles += (uint64_t)((f->width + TW - 1) / TW) * ((f->height + TH - 1) / TH);
   }
   if (sc[n_scenes - 1].first_renderable + sc[n_scenes - 1].n_renderables != n_rs)
     return fail(c, MR_E_INVALID, "scene renderable ranges must cover every renderable");
@@ -805,7 +814,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   CK(B.tiles.ensure(3 * tiles + 1), "batch tiles");
   if (B.bins.cap < std::max<size_t>((size_t)1 << 20, 2 * tris))
     CK(B.bins.ensure(std::max<size_t>((size_t)1 << 20, 2 * tris)), "batch bins");
-  int grid = batch_grid(B.tile, B.chunk, B.threads);
+  int grid = batch_grid(TW, TH, B.chunk, B.threads);
   if (grid <= 0) return fail(c, MR_E_INVALID, "batch tuning does not fit on the device");
   CK(B.block_sums.ensure((size_t)grid + 1), "batch scan");
   uint32_t tri = 0, vb = 0, nb = 0, tile_base = 0;
@@ -814,8 +823,8 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
     SceneRec& SR = B.h_scenes[s];
     memset(&SR, 0, sizeof(SR));
     make_view(f, SR.v);
-    SR.tiles_x = (f->width + TS - 1) / TS;
-    SR.tiles_y = (f->height + TS - 1) / TS;
+    SR.tiles_x = (f->width + TW - 1) / TW;
+    SR.tiles_y = (f->height + TH - 1) / TH;
     SR.tile_base = tile_base;
     stb[s] = tile_base;
     tile_base += (uint32_t)(SR.tiles_x * SR.tiles_y);
@@ -881,7 +890,8 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   P.scene_tile_base = B.bases.p + 3 * (n_rs + 1);
   P.n_scenes = n_scenes;
   P.n_tiles = tile_base;
-  P.tile = TS;
+  P.tile_w = TW;
+  P.tile_h = TH;
   P.chunk = B.chunk;
   P.recs = B.recs.p;
   P.rec_cap = (uint32_t)std::min<size_t>(B.recs.cap, 0xFFFFFFFFu);

@@ -20,7 +20,12 @@ cudaError_t launch_range(int W, int H, const float* dP, const float* depth, floa
                          cudaStream_t st);
 cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
                          cudaEvent_t* ev);
-int batch_grid(int tile, int chunk, int threads);
+int batch_grid(int tile_w, int tile_h, int chunk, int threads);
+// Tile shapes k_batch takes: power-of-two sides, 64..1024 pixels (whole warps).
+inline bool batch_tile_ok(int tw, int th) {
+  auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
+  return pow2(tw) && pow2(th) && tw >= 4 && tw <= 256 && th >= 2 && th <= 32 && tw * th >= 64 && tw * th <= 1024;
+}
 }  // namespace mrg
 
 using namespace mrg;
@@ -76,7 +81,7 @@ using namespace mrgi;
 // and (optionally) the CUDA graph of its launch sequence.  The context owns
 // one for mr_render_batch; a render server owns several.
 struct BatchSlot {
-  int tile = 16, threads = 256, chunk = 64;
+  int tile_w = 16, tile_h = 16, threads = 256, chunk = 64;
   bool graphs = true;
   DevBuf<DevRenderable> rs;
   DevBuf<uint32_t> bases;

@@ -226,7 +226,8 @@ __device__ __forceinline__ bool covered(float e1, float e2) {
 }
 
 // Walks columns xs..xe of row y (replaying the running sums from x0) and
-// calls emit(x, packed) for every fragment that would pass z < 1e11f.
+// calls emit(x, packed, e1, e2) for every fragment that would pass z < 1e11f
+// (e1, e2: the running edge values at column x).
 template <typename Emit>
 __device__ __forceinline__ void walk_row(const Setup& S, bool persp, uint32_t id, int y, int xs,
                                          int xe, Emit emit) {
@@ -241,7 +242,7 @@ __device__ __forceinline__ void walk_row(const Setup& S, bool persp, uint32_t id
     if (covered(e1, e2)) {
       float k0, k1, k2;
       float z = frag_depth(S, persp, e1, e2, k0, k1, k2);
-      if (z < 1e11f) emit(x, ((unsigned long long)depth_key(z) << 32) | id);
+      if (z < 1e11f) emit(x, ((unsigned long long)depth_key(z) << 32) | id, e1, e2);
     }
     e1 += d1;
     e2 += d2;
@@ -327,61 +328,39 @@ __device__ __forceinline__ bool setup_triangle(const View& V, const Geo& G, cons
   return true;
 }
 
-// Shading of the pixel (x, y) whose visibility word is vw, src/Renderer.cpp:
-// 247-305 (FAST_LIGHT): re-derives the winner's setup, replays its edge
-// functions to column x, and evaluates texture and Blinn-Phong lighting.
+// The sub-triangle `id` won by a pixel: its renderable, vertex indices and
+// view-space corners with attributes (the clipped sub-triangle when the
+// triangle crosses the near plane), src/Renderer.cpp:334-379, 131-161.
 // Renderables of the pixel's frame are rs_lo..rs_hi-1.
+// s_tb, when given, holds tri_base[rs_lo .. rs_hi) in shared memory.
 template <bool PRE>
-__device__ __forceinline__ void resolve_pixel(const View& V, const Geo& G, int rs_lo, int rs_hi,
-                                              unsigned long long vw, int x, int y, const float* s_dec,
-                                              V3& value, float& depth, uint32_t& id, V3& normal_out) {
-  normal_out = v3(0, 0, 1);
-  if (vw == VIS_EMPTY) {
-    value = v3(V.bg[0], V.bg[1], V.bg[2]);
-    depth = 1e11f;
-    id = MR_NO_TRIANGLE;
-    return;
-  }
-  id = (uint32_t)vw;
+__device__ __forceinline__ const DevRenderable* winner_tri(const View& V, const Geo& G, int rs_lo, int rs_hi,
+                                                         uint32_t id, int (&ip)[3], Vtx (&vc)[3],
+                                                         bool& clipped, const uint32_t* s_tb = nullptr) {
   const uint32_t g = id >> 1;
   const int s = (int)(id & 1u);
-  const DevRenderable& R = G.rs[find_base(G.tri_base, rs_lo, rs_hi, g)];
-  const int t = (int)(g - R.tri_base);
-  int ip[3];
+  const int k = s_tb ? rs_lo + find_base(s_tb, 0, rs_hi - rs_lo, g) : find_base(G.tri_base, rs_lo, rs_hi, g);
+  const DevRenderable* R = &G.rs[k];
+  const int t = (int)(g - R->tri_base);
 #pragma unroll
-  for (int c = 0; c < 3; c++) ip[c] = __ldg(R.mesh.idx + 3 * t + c);
-  Vtx vc[3];
-  corners<PRE, true>(G, R, t, ip, vc);
-  Setup S;
+  for (int c = 0; c < 3; c++) ip[c] = __ldg(R->mesh.idx + 3 * t + c);
+  corners<PRE, true>(G, *R, t, ip, vc);
   const float zn = V.znear;
-  if (vc[0].pos.z > zn || vc[1].pos.z > zn || vc[2].pos.z > zn) {
+  clipped = vc[0].pos.z > zn || vc[1].pos.z > zn || vc[2].pos.z > zn;
+  if (clipped) {
     Vtx sub[2][3];
     clip_tri<true>(zn, vc, sub);
     // sub-triangle s exists: it won this pixel
 #pragma unroll
     for (int c = 0; c < 3; c++) vc[c] = s ? sub[1][c] : sub[0][c];
-    setup_view(V, vc, S);
-  } else if (PRE) {
-    V2 p[3];
-    float zt[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      float4 a = G.va[R.vert_base + ip[c]];
-      p[c] = v2(a.x, a.y);
-      zt[c] = a.z;
-    }
-    setup_from(V, p, zt, S);
-  } else {
-    setup_view(V, vc, S);
   }
-  float e1, e2;
-  row_start(S, y, e1, e2);
-  for (int c = S.x0; c < x; c++) {
-    e1 += S.n1.x;
-    e2 += S.n2.x;
-  }
-  float k0, k1, k2;
-  depth = frag_depth(S, V.persp != 0, e1, e2, k0, k1, k2);
+  return R;
+}
+
+// Texture and Blinn-Phong lighting of a fragment with perspective-corrected
+// weights k0..k2 over the corners vc, src/Renderer.cpp:262-305 (FAST_LIGHT).
+__device__ __forceinline__ void shade(const View& V, const DevRenderable& R, const Vtx (&vc)[3], float k0,
+                                      float k1, float k2, const float* s_dec, V3& value, V3& normal_out) {
   V3 color = v3(R.diffuse[0], R.diffuse[1], R.diffuse[2]);
   if (R.has_tex) {
     V2 uv = add2(add2(ks2(k0, vc[0].uv), ks2(k1, vc[1].uv)), ks2(k2, vc[2].uv));
@@ -411,6 +390,69 @@ __device__ __forceinline__ void resolve_pixel(const View& V, const Geo& G, int r
     }
     normal_out = normal;
   }
+}
+
+// Depth terms of the winning sub-triangle's corners: the values its setup
+// used (src/Renderer.cpp:223-224).
+template <bool PRE>
+__device__ __forceinline__ void winner_zterms(const View& V, const Geo& G, const DevRenderable& R,
+                                              const int (&ip)[3], const Vtx (&vc)[3], bool clipped,
+                                              float (&zt)[3]) {
+  if (PRE && !clipped) {
+#pragma unroll
+    for (int c = 0; c < 3; c++) zt[c] = G.va[R.vert_base + ip[c]].z;
+  } else {
+    float px, py;
+#pragma unroll
+    for (int c = 0; c < 3; c++) project(V, vc[c].pos, px, py, zt[c]);
+  }
+}
+
+// Shading of the pixel (x, y) whose visibility word is vw, src/Renderer.cpp:
+// 247-305 (FAST_LIGHT): re-derives the winner's setup, replays its edge
+// functions to column x, and evaluates texture and Blinn-Phong lighting.
+// Renderables of the pixel's frame are rs_lo..rs_hi-1.
+template <bool PRE>
+__device__ __forceinline__ void resolve_pixel(const View& V, const Geo& G, int rs_lo, int rs_hi,
+                                              unsigned long long vw, int x, int y, const float* s_dec,
+                                              V3& value, float& depth, uint32_t& id, V3& normal_out) {
+  normal_out = v3(0, 0, 1);
+  if (vw == VIS_EMPTY) {
+    value = v3(V.bg[0], V.bg[1], V.bg[2]);
+    depth = 1e11f;
+    id = MR_NO_TRIANGLE;
+    return;
+  }
+  id = (uint32_t)vw;
+  int ip[3];
+  Vtx vc[3];
+  bool clipped;
+  const DevRenderable& R = *winner_tri<PRE>(V, G, rs_lo, rs_hi, id, ip, vc, clipped);
+  Setup S;
+  if (clipped) {
+    setup_view(V, vc, S);
+  } else if (PRE) {
+    V2 p[3];
+    float zt[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float4 a = G.va[R.vert_base + ip[c]];
+      p[c] = v2(a.x, a.y);
+      zt[c] = a.z;
+    }
+    setup_from(V, p, zt, S);
+  } else {
+    setup_view(V, vc, S);
+  }
+  float e1, e2;
+  row_start(S, y, e1, e2);
+  for (int c = S.x0; c < x; c++) {
+    e1 += S.n1.x;
+    e2 += S.n2.x;
+  }
+  float k0, k1, k2;
+  depth = frag_depth(S, V.persp != 0, e1, e2, k0, k1, k2);
+  shade(V, R, vc, k0, k1, k2, s_dec, value, normal_out);
 }
 
 // savePPM conversion, src/io.cpp:358-362.
@@ -531,7 +573,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
         if (kind[s] == 1) {
           const uint32_t id = 2u * g + (uint32_t)s;
           for (int y = S[s].y0; y <= S[s].y1; y++)
-            walk_row(S[s], persp, id, y, S[s].x0, S[s].x1, [&](int x, unsigned long long v) {
+            walk_row(S[s], persp, id, y, S[s].x0, S[s].x1, [&](int x, unsigned long long v, float, float) {
               atomicMin(vis + (size_t)y * W + x, v);
             });
         }
@@ -584,7 +626,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
         T.z[0] = q.z0; T.z[1] = q.z1; T.z[2] = q.z2;
         T.x0 = q.x0; T.x1 = q.x1; T.y0 = q.y0;
         const int y = q.y0 + (k - s_pre[w][lo]);
-        walk_row(T, persp, q.id, y, T.x0, T.x1, [&](int x, unsigned long long v) {
+        walk_row(T, persp, q.id, y, T.x0, T.x1, [&](int x, unsigned long long v, float, float) {
           atomicMin(vis + (size_t)y * W + x, v);
         });
       }
@@ -616,7 +658,7 @@ __device__ __forceinline__ void raster_into_tile(const BigRec* recs, const uint3
     int xs = max(B.x0, px0), xe = min(B.x1, px1);
     if (xs > xe) continue;
     Setup S = rec_setup(B);
-    walk_row(S, persp, B.id, y, xs, xe, [&](int x, unsigned long long v) {
+    walk_row(S, persp, B.id, y, xs, xe, [&](int x, unsigned long long v, float, float) {
       atomicMin(svis + (y - py0) * TS + (x - px0), v);
     });
   }
@@ -778,7 +820,7 @@ __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
         B.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
         B.rec_scene[slot] = scene;
         const SceneRec& SR = B.scenes[scene];
-        int tx0 = S[s].x0 / B.tile, tx1 = S[s].x1 / B.tile, ty0 = S[s].y0 / B.tile, ty1 = S[s].y1 / B.tile;
+        int tx0 = S[s].x0 / B.tile_w, tx1 = S[s].x1 / B.tile_w, ty0 = S[s].y0 / B.tile_h, ty1 = S[s].y1 / B.tile_h;
         for (int ty = ty0; ty <= ty1; ty++)
           for (int tx = tx0; tx <= tx1; tx++)
             atomicAdd(B.tile_count + SR.tile_base + ty * SR.tiles_x + tx, 1u);
@@ -791,6 +833,122 @@ __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
   block_flush(bc, &B.counters->rasterised, nullptr, &B.counters->clipped);
 }
 
+// Renderables per scene whose triangle bases k_batch keeps in shared memory
+// (larger scenes search the global table).
+constexpr int kBatchTbMax = 256;
+
+// Exclusive prefix sum of v over the threads of the block (blockDim.x a
+// multiple of 32, at most 1024); tot = the block's sum.  Every thread of the
+// block must call it; s_part holds 33 words.
+__device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_part, uint32_t& tot) {
+  const int lane = (int)(threadIdx.x & 31), w = (int)(threadIdx.x >> 5), nw = (int)(blockDim.x >> 5);
+  uint32_t inc = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+    if (lane >= o) inc += u;
+  }
+  __syncthreads();  // s_part free from a previous call
+  if (lane == 31) s_part[w] = inc;
+  __syncthreads();
+  if (w == 0) {
+    const uint32_t p = lane < nw ? s_part[lane] : 0u;
+    uint32_t pi = p;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t u = __shfl_up_sync(0xffffffffu, pi, o);
+      if (lane >= o) pi += u;
+    }
+    if (lane < nw) s_part[lane] = pi - p;
+    if (lane == 31) s_part[32] = pi;
+  }
+  __syncthreads();
+  tot = s_part[32];
+  return s_part[w] + inc - v;
+}
+
+// Stages the tile's records bins[c0 .. c0+cn) in shared memory with the
+// exclusive prefix of the rows each covers inside the tile (px0..px1,
+// py0..py1): s_off[cn] is the number of (record, row) items.  Block-wide.
+__device__ __forceinline__ void stage_chunk(const BigRec* recs, const uint32_t* bins, uint32_t c0, uint32_t cn,
+                                            int px0, int py0, int px1, int py1, BigRec* s_recs,
+                                            uint32_t* s_off) {
+  __syncthreads();  // the previous pass over s_recs / s_off is done
+  for (uint32_t i = threadIdx.x; i < cn; i += blockDim.x) {
+    const BigRec r = recs[bins[c0 + i]];
+    s_recs[i] = r;
+    const int ys = max(r.y0, py0), ye = min(r.y1, py1);
+    const bool hit = ys <= ye && max(r.x0, px0) <= min(r.x1, px1);
+    s_off[i] = hit ? (uint32_t)(ye - ys + 1) : 0u;
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) {  // one warp scans: each lane a contiguous run
+    const int lane = (int)threadIdx.x;
+    const uint32_t per = (cn + 31) / 32;
+    const uint32_t b = min(cn, (uint32_t)lane * per), e = min(cn, b + per);
+    uint32_t sum = 0;
+    for (uint32_t i = b; i < e; i++) sum += s_off[i];
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t u = __shfl_up_sync(0xffffffffu, inc, o);
+      if (lane >= o) inc += u;
+    }
+    uint32_t run = inc - sum;
+    for (uint32_t i = b; i < e; i++) {
+      const uint32_t c = s_off[i];
+      s_off[i] = run;
+      run += c;
+    }
+    if (lane == 31) s_off[cn] = inc;
+  }
+  __syncthreads();
+}
+
+// The (record, row) items of a staged chunk, one per thread: CAPTURE=false
+// merges the fragments into the shared visibility tile; CAPTURE=true (after
+// every record of the tile has been merged) stores, for each pixel, the
+// running edge values of the fragment that won it, so the resolve needs no
+// replay.  A pixel's winning word is unique (it holds the sub-triangle id).
+template <bool CAPTURE>
+__device__ __forceinline__ void raster_items(const BigRec* s_recs, const uint32_t* s_off, uint32_t cn, int TW,
+                                             int px0, int py0, int px1, int py1, bool persp,
+                                             unsigned long long* svis, float2* s_e) {
+  const uint32_t total = s_off[cn];
+  for (uint32_t it = threadIdx.x; it < total; it += blockDim.x) {
+    int lo = 0, hi = (int)cn;  // s_off[lo] <= it < s_off[hi]
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if (s_off[mid] <= it) lo = mid; else hi = mid;
+    }
+    const BigRec& R = s_recs[lo];
+    const int y = max(R.y0, py0) + (int)(it - s_off[lo]);
+    const int xs = max(R.x0, px0), xe = min(R.x1, px1);
+    const Setup S = rec_setup(R);
+    if (CAPTURE) {
+      // the fragment that won a pixel is the one whose id the pixel holds
+      // (it was covered and passed the depth test in the first pass)
+      float e1, e2;
+      row_start(S, y, e1, e2);
+      const float d1 = S.n1.x, d2 = S.n2.x;
+      for (int x = S.x0; x < xs; x++) {
+        e1 += d1;
+        e2 += d2;
+      }
+      const uint32_t* row = reinterpret_cast<const uint32_t*>(svis + (y - py0) * TW);  // low words: ids
+      for (int x = xs; x <= xe; x++) {
+        if (row[2 * (x - px0)] == R.id) s_e[(y - py0) * TW + (x - px0)] = make_float2(e1, e2);
+        e1 += d1;
+        e2 += d2;
+      }
+    } else {
+      walk_row(S, persp, R.id, y, xs, xe, [&](int x, unsigned long long v, float, float) {
+        atomicMin(svis + (y - py0) * TW + (x - px0), v);
+      });
+    }
+  }
+}
+
 // The batch's persistent kernel (cooperative launch, grid-wide barriers):
 //   1. exclusive scan of the per-tile counts (per-block segments + one block
 //      scanning the block sums), 2. scatter record indices into tile lists,
@@ -798,52 +956,68 @@ __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
 //      staged in shared memory `chunk` at a time and rasterised into a
 //      shared-memory visibility tile, then every pixel of the tile is
 //      resolved, shaded and written to its scene's outputs.
-__global__ void __launch_bounds__(256, 2) k_batch(BatchParams B, uint32_t* block_sums) {
+// MINB: blocks of 256 threads per SM the register allocation must allow
+// (2: up to 128 registers per thread, for 64-thread blocks; 4: up to 64, so
+// that 128- and 256-thread blocks keep enough warps resident).
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* block_sums) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int TS = B.tile;
+  const int TW = B.tile_w, TH = B.tile_h, TP = TW * TH;
   unsigned long long* svis = (unsigned long long*)smem;
-  BigRec* s_recs = (BigRec*)(smem + (size_t)TS * TS * sizeof(unsigned long long));
+  float2* s_e = (float2*)(smem + (size_t)TP * sizeof(unsigned long long));
+  BigRec* s_recs = (BigRec*)(smem + (size_t)TP * (sizeof(unsigned long long) + sizeof(float2)));
+  uint32_t* s_off = (uint32_t*)(s_recs + B.chunk);  // chunk + 1 entries
   __shared__ float s_dec[256];
-  __shared__ uint32_t s_part[32];
+  __shared__ uint32_t s_part[33];
   __shared__ uint32_t s_tile;
   __shared__ View s_view;
   __shared__ int s_meta[8];
+  __shared__ uint32_t s_tb[kBatchTbMax];
+  __shared__ int s_tb_scene;
+  __shared__ uint8_t* s_out8;
+  __shared__ float* s_outd;
+  __shared__ uint32_t* s_outi;
   cg::grid_group grid = cg::this_grid();
   const uint32_t nb = gridDim.x, nt = blockDim.x;
   for (uint32_t i = threadIdx.x; i < 256; i += nt) s_dec[i] = (float)i / 255.0f;
+  if (threadIdx.x == 0) s_tb_scene = -1;
   // 1. scan: block b owns tiles [b*seg, (b+1)*seg)
   const uint32_t seg = (B.n_tiles + nb - 1) / nb;
   const uint32_t t0 = min(B.n_tiles, blockIdx.x * seg), t1 = min(B.n_tiles, t0 + seg);
   {
     uint32_t sum = 0;
     for (uint32_t i = t0 + threadIdx.x; i < t1; i += nt) sum += B.tile_count[i];
-    sum = __reduce_add_sync(0xffffffffu, sum);
-    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = sum;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      uint32_t tot = 0;
-      for (uint32_t w = 0; w < (nt + 31) / 32; w++) tot += s_part[w];
-      block_sums[blockIdx.x] = tot;
-    }
+    uint32_t tot;
+    block_scan(sum, s_part, tot);
+    if (threadIdx.x == 0) block_sums[blockIdx.x] = tot;
   }
   grid.sync();
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
+  if (blockIdx.x == 0) {  // exclusive scan of the block sums, by the whole block
     uint32_t run = 0;
-    for (uint32_t i = 0; i < nb; i++) {
-      uint32_t v = block_sums[i];
-      block_sums[i] = run;
-      run += v;
+    for (uint32_t b0 = 0; b0 < nb; b0 += nt) {
+      const uint32_t i = b0 + threadIdx.x;
+      const uint32_t v = i < nb ? block_sums[i] : 0u;
+      uint32_t tot;
+      const uint32_t ex = block_scan(v, s_part, tot);
+      if (i < nb) block_sums[i] = run + ex;
+      run += tot;
     }
-    B.tile_start[B.n_tiles] = run;
-    B.counters->bin_needed = run;
-    B.counters->bin_entries += run;
+    if (threadIdx.x == 0) {
+      B.tile_start[B.n_tiles] = run;
+      B.counters->bin_needed = run;
+      B.counters->bin_entries += run;
+    }
   }
   grid.sync();
-  if (threadIdx.x == 0) {
+  {
     uint32_t run = block_sums[blockIdx.x];
-    for (uint32_t i = t0; i < t1; i++) {
-      B.tile_start[i] = run;
-      run += B.tile_count[i];
+    for (uint32_t b0 = t0; b0 < t1; b0 += nt) {
+      const uint32_t i = b0 + threadIdx.x;
+      const uint32_t v = i < t1 ? B.tile_count[i] : 0u;
+      uint32_t tot;
+      const uint32_t ex = block_scan(v, s_part, tot);
+      if (i < t1) B.tile_start[i] = run + ex;
+      run += tot;
     }
   }
   grid.sync();
@@ -852,7 +1026,7 @@ __global__ void __launch_bounds__(256, 2) k_batch(BatchParams B, uint32_t* block
   for (uint32_t i = blockIdx.x * nt + threadIdx.x; i < nrec; i += nb * nt) {
     const BigRec& R = B.recs[i];
     const SceneRec& SR = B.scenes[B.rec_scene[i]];
-    int tx0 = R.x0 / TS, tx1 = R.x1 / TS, ty0 = R.y0 / TS, ty1 = R.y1 / TS;
+    int tx0 = R.x0 / TW, tx1 = R.x1 / TW, ty0 = R.y0 / TH, ty1 = R.y1 / TH;
     for (int ty = ty0; ty <= ty1; ty++)
       for (int tx = tx0; tx <= tx1; tx++) {
         uint32_t t = SR.tile_base + ty * SR.tiles_x + tx;
@@ -865,53 +1039,97 @@ __global__ void __launch_bounds__(256, 2) k_batch(BatchParams B, uint32_t* block
   // 3. tiles
   for (;;) {
     __syncthreads();
-    if (threadIdx.x == 0) {
-      s_tile = atomicAdd(&B.counters->work_next, 1u);
-      if (s_tile < B.n_tiles) {
-        int sc = find_base(B.scene_tile_base, 0, B.n_scenes, s_tile);
+    if (threadIdx.x < 32) {  // warp 0 takes the next tile and loads its scene
+      const int lane = (int)threadIdx.x;
+      uint32_t t = 0;
+      if (lane == 0) t = atomicAdd(&B.counters->work_next, 1u);
+      t = __shfl_sync(0xffffffffu, t, 0);
+      if (t < B.n_tiles) {
+        // the scene: the last j with scene_tile_base[j] <= t (bases ascending)
+        unsigned cnt = 0;
+        for (int j = 1 + lane; j < B.n_scenes; j += 32) cnt += B.scene_tile_base[j] <= t;
+        const int sc = (int)__reduce_add_sync(0xffffffffu, cnt);
         const SceneRec& SR = B.scenes[sc];
-        s_view = SR.v;
-        s_meta[0] = sc;
-        s_meta[1] = (int)(s_tile - SR.tile_base);
-        s_meta[2] = SR.tiles_x;
-        s_meta[3] = (int)SR.rs_begin;
-        s_meta[4] = (int)SR.rs_end;
-        s_meta[5] = (int)(2u * B.g.tri_base[SR.rs_begin]);  // ids are reported per scene
+        const uint32_t* src = reinterpret_cast<const uint32_t*>(&SR.v);
+        uint32_t* dst = reinterpret_cast<uint32_t*>(&s_view);
+        for (int k = lane; k < (int)(sizeof(View) / 4); k += 32) dst[k] = src[k];
+        if (lane == 0) {
+          s_meta[0] = sc;
+          s_meta[1] = (int)(t - SR.tile_base);
+          s_meta[2] = SR.tiles_x;
+          s_meta[3] = (int)SR.rs_begin;
+          s_meta[4] = (int)SR.rs_end;
+          s_meta[5] = (int)(2u * B.g.tri_base[SR.rs_begin]);  // ids are reported per scene
+          // the tile's list (bins truncated at capacity on overflow)
+          s_meta[6] = (int)min(B.tile_start[t], B.bin_cap);
+          s_meta[7] = (int)min(B.tile_start[t + 1], B.bin_cap);
+          s_out8 = SR.rgb8;
+          s_outd = SR.depth;
+          s_outi = SR.ids;
+        }
       }
+      if (lane == 0) s_tile = t;
     }
     __syncthreads();
     const uint32_t tile = s_tile;
     if (tile >= B.n_tiles) break;
-    for (int i = threadIdx.x; i < TS * TS; i += nt) svis[i] = VIS_EMPTY;
-    const SceneRec& SR = B.scenes[s_meta[0]];
+    for (int i = threadIdx.x; i < TP; i += nt) svis[i] = VIS_EMPTY;
+    const int n_rs = s_meta[4] - s_meta[3];
+    const bool tb_shared = n_rs <= kBatchTbMax;
+    if (tb_shared && s_tb_scene != s_meta[0]) {  // uniform: read after the barrier above
+      for (int i = threadIdx.x; i < n_rs; i += nt) s_tb[i] = B.g.tri_base[s_meta[3] + i];
+      __syncthreads();
+      if (threadIdx.x == 0) s_tb_scene = s_meta[0];
+    }
     const int lt = s_meta[1], tx = lt % s_meta[2], ty = lt / s_meta[2];
-    const int px0 = tx * TS, py0 = ty * TS;
-    const int px1 = min(px0 + TS, s_view.W) - 1, py1 = min(py0 + TS, s_view.H) - 1;
-    const uint32_t s = B.tile_start[tile], e = min(B.tile_start[tile + 1], B.bin_cap);
+    const int px0 = tx * TW, py0 = ty * TH;
+    const int px1 = min(px0 + TW, s_view.W) - 1, py1 = min(py0 + TH, s_view.H) - 1;
+    const uint32_t s = (uint32_t)s_meta[6], e = (uint32_t)s_meta[7];
     const bool persp = s_view.persp != 0;
-    for (uint32_t c0 = s; c0 < e; c0 += B.chunk) {
-      const uint32_t cn = min((uint32_t)B.chunk, e - c0);
-      __syncthreads();
-      for (uint32_t i = threadIdx.x; i < cn; i += nt) s_recs[i] = B.recs[B.bins[c0 + i]];
-      __syncthreads();
-      raster_into_tile(s_recs, nullptr, 0, cn, TS, px0, py0, px1, py1, persp, svis);
+    const uint32_t nck = (e - s + (uint32_t)B.chunk - 1) / (uint32_t)B.chunk;
+    for (uint32_t c = 0; c < nck; c++) {  // pass 1: depth test
+      const uint32_t c0 = s + c * (uint32_t)B.chunk, cn = min((uint32_t)B.chunk, e - c0);
+      stage_chunk(B.recs, B.bins, c0, cn, px0, py0, px1, py1, s_recs, s_off);
+      raster_items<false>(s_recs, s_off, cn, TW, px0, py0, px1, py1, persp, svis, s_e);
+    }
+    for (uint32_t c = 0; c < nck; c++) {  // pass 2: the winners' edge values
+      const uint32_t c0 = s + c * (uint32_t)B.chunk, cn = min((uint32_t)B.chunk, e - c0);
+      if (nck > 1) stage_chunk(B.recs, B.bins, c0, cn, px0, py0, px1, py1, s_recs, s_off);
+      else __syncthreads();
+      raster_items<true>(s_recs, s_off, cn, TW, px0, py0, px1, py1, persp, svis, s_e);
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < TS * TS; i += nt) {
-      const int x = px0 + i % TS, y = py0 + i / TS;
+    for (int i = threadIdx.x; i < TP; i += nt) {
+      const int x = px0 + i % TW, y = py0 + i / TW;
       if (x > px1 || y > py1) continue;
+      const unsigned long long vw = svis[i];
       V3 value, normal;
       float depth;
-      uint32_t id;
-      resolve_pixel<true>(s_view, B.g, s_meta[3], s_meta[4], svis[i], x, y, s_dec, value, depth, id, normal);
-      const size_t px = (size_t)y * s_view.W + x;
-      if (SR.rgb8) {
-        SR.rgb8[3 * px + 0] = to_byte(value.x);
-        SR.rgb8[3 * px + 1] = to_byte(value.y);
-        SR.rgb8[3 * px + 2] = to_byte(value.z);
+      const uint32_t id = (uint32_t)vw;
+      if (vw == VIS_EMPTY) {
+        value = v3(s_view.bg[0], s_view.bg[1], s_view.bg[2]);
+        depth = 1e11f;
+      } else {
+        int ip[3];
+        Vtx vc[3];
+        bool clipped;
+        const DevRenderable& R = *winner_tri<true>(s_view, B.g, s_meta[3], s_meta[4], id, ip, vc, clipped,
+                                                   tb_shared ? s_tb : nullptr);
+        Setup S;
+        winner_zterms<true>(s_view, B.g, R, ip, vc, clipped, S.z);
+        const float2 ee = s_e[i];
+        float k0, k1, k2;
+        depth = frag_depth(S, persp, ee.x, ee.y, k0, k1, k2);
+        shade(s_view, R, vc, k0, k1, k2, s_dec, value, normal);
       }
-      if (SR.depth) SR.depth[px] = depth;
-      if (SR.ids) SR.ids[px] = id == MR_NO_TRIANGLE ? id : id - (uint32_t)s_meta[5];
+      const size_t px = (size_t)y * s_view.W + x;
+      if (uint8_t* o8 = s_out8) {
+        o8[3 * px + 0] = to_byte(value.x);
+        o8[3 * px + 1] = to_byte(value.y);
+        o8[3 * px + 2] = to_byte(value.z);
+      }
+      if (s_outd) s_outd[px] = depth;
+      if (s_outi) s_outi[px] = vw == VIS_EMPTY ? MR_NO_TRIANGLE : id - (uint32_t)s_meta[5];
     }
   }
 }
@@ -1011,23 +1229,24 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   return cudaGetLastError();
 }
 
-size_t batch_smem(int tile, int chunk) {
-  return (size_t)tile * tile * sizeof(unsigned long long) + (size_t)chunk * sizeof(BigRec);
+size_t batch_smem(int tile_w, int tile_h, int chunk) {
+  // visibility words + captured edge values per pixel, staged records, row prefix
+  return (size_t)tile_w * tile_h * (sizeof(unsigned long long) + sizeof(float2)) + (size_t)chunk * sizeof(BigRec) +
+         (size_t)(chunk + 1) * sizeof(uint32_t);
 }
-
+static const void* batch_kernel(int threads) {
+  return threads <= 64 ? (const void*)k_batch<2> : (const void*)k_batch<4>;
+}
 // Co-resident blocks of k_batch for the given shape (its cooperative grid).
-int batch_grid(int tile, int chunk, int threads) {
+int batch_grid(int tile_w, int tile_h, int chunk, int threads) {
   int per = 0;
-  size_t smem = batch_smem(tile, chunk);
-  cudaFuncSetAttribute(k_batch, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch, threads, smem);
+  size_t smem = batch_smem(tile_w, tile_h, chunk);
+  const void* k = batch_kernel(threads);
+  cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, threads, smem);
   if (per <= 0) return 0;
   return sm_count() * per;
 }
-
-// Launch sequence of a batch: vertex pass, setup + tile counts, persistent
-// fused kernel.  block_sums holds grid + 1 words.  ev (optional, 4 events)
-// brackets vertex pass, setup, fused kernel.
 cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
                          cudaEvent_t* ev) {
   if (ev) cudaEventRecord(ev[0], st);
@@ -1040,7 +1259,8 @@ cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* 
   if (ev) cudaEventRecord(ev[2], st);
   BatchParams Bc = B;
   void* args[] = {&Bc, &block_sums};
-  cudaError_t e = launch_coop((const void*)k_batch, grid, threads, args, batch_smem(B.tile, B.chunk), st);
+  cudaError_t e = launch_coop(batch_kernel(threads), grid, threads, args, batch_smem(B.tile_w, B.tile_h, B.chunk),
+                              st);
   if (ev) cudaEventRecord(ev[3], st);
   if (e != cudaSuccess) return e;
   return cudaGetLastError();

@@ -131,7 +131,7 @@ struct BatchParams {
   const uint32_t* scene_tile_base;  // n_scenes + 1 prefix of tile counts
   int n_scenes;
   uint32_t n_tiles;
-  int tile, chunk;                  // tile edge, records staged per pass
+  int tile_w, tile_h, chunk;        // tile width and height (pixels), records staged per pass
   BigRec* recs;
   uint32_t rec_cap;
   uint32_t* rec_scene;              // scene of each record

@@ -324,15 +324,20 @@ extern "C" {
 
 MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out) {
   if (!c || !o || !out || o->slots < 1 || o->max_batch < 1 || o->budget_bytes == 0) return MR_E_INVALID;
+  const int tw = o->tile ? o->tile : 16, th = o->tile_h ? o->tile_h : tw;
+  const int threads = o->threads ? o->threads : 64, chunk = o->chunk ? o->chunk : 64;
+  if (!batch_tile_ok(tw, th) || (threads != 64 && threads != 128 && threads != 256) || chunk < 16 || chunk > 256)
+    return MR_E_INVALID;
   mr_server* s = new mr_server();
   s->c = c;
   s->o = *o;
   cudaSetDevice(c->device);
   for (int i = 0; i < o->slots; i++) {
     Slot* sl = new Slot();
-    sl->b.tile = o->tile ? o->tile : 16;
-    sl->b.threads = o->threads ? o->threads : 64;
-    sl->b.chunk = o->chunk ? o->chunk : 64;
+    sl->b.tile_w = tw;
+    sl->b.tile_h = th;
+    sl->b.threads = threads;
+    sl->b.chunk = chunk;
     sl->b.graphs = false;  // shapes change from batch to batch
     if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess) {
       delete sl;

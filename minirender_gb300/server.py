@@ -16,9 +16,11 @@ from .scene import Material, TriMesh
 
 class RenderServer:
     def __init__(self, ctx: capi.Context, budget_bytes: int = 40 << 30, slots: int = 2, max_batch: int = 32,
-                 tile: int = 16, threads: int = 64, chunk: int = 64):
+                 tile: int = 16, threads: int = 64, chunk: int = 64, tile_h: int = 0):
+        """tile x tile_h screen tiles (tile_h 0: square), threads per tile
+        block and records per shared-memory pass of the fused batch kernel."""
         self.ctx = ctx
-        o = abi.mr_server_opts(budget_bytes, slots, max_batch, tile, threads, chunk)
+        o = abi.mr_server_opts(budget_bytes, slots, max_batch, tile, threads, chunk, tile_h)
         h = C.c_void_p()
         rc = capi.lib().mr_server_create(ctx.h, C.byref(o), C.byref(h))
         if rc != 0:

@@ -79,6 +79,24 @@ def test_graph_replay_with_new_cameras(batch, refs):
     _check_all(batch, moved, new_refs, "replay")
 
 
+@pytest.mark.parametrize("tw,th,threads,chunk", [(64, 16, 128, 128), (128, 8, 64, 32), (256, 4, 256, 64),
+                                                  (4, 16, 64, 16)])
+def test_batch_rectangular_tiles_same_result(batch, refs, tw, th, threads, chunk):
+    batch.ctx.set_batch_graphs(True)
+    batch.ctx.set_batch_tiling(tw, th, threads, chunk)
+    try:
+        _check_all(batch, _items(), refs, f"r{tw}x{th}_{threads}_{chunk}")
+    finally:
+        batch.ctx.set_batch_tuning(16, 256, 64)
+
+
+def test_batch_tiling_rejects_bad_shapes(batch):
+    from minirender_gb300 import capi
+    for bad in [(48, 16, 64, 64), (512, 2, 64, 64), (8, 4, 64, 64), (64, 32, 64, 64), (16, 16, 96, 64)]:
+        with pytest.raises(capi.MRError):
+            batch.ctx.set_batch_tiling(*bad)
+
+
 @pytest.mark.parametrize("tile,threads,chunk", [(8, 64, 16), (16, 128, 256), (32, 256, 32), (32, 128, 128)])
 def test_batch_tuning_same_result(batch, refs, tile, threads, chunk):
     batch.ctx.set_batch_graphs(True)
