@@ -25,6 +25,7 @@ from __future__ import annotations
 
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -50,6 +51,8 @@ def parse():
     p.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4", "config5"])
     p.add_argument("--rates", default="100,500,1000,2000,5000", help="request rates swept (config5)")
     p.add_argument("--requests", type=int, default=1500, help="requests per rate (config5)")
+    p.add_argument("--serve-tuning", default="16,16,64,64",
+                   help="tile_w,tile_h,threads,chunk of the render server's batches (config5)")
     p.add_argument("--scenes", type=int, default=256, help="scenes per batch (config4)")
     p.add_argument("--tuning", default="",
                    help="tile,threads,chunk or tile_w,tile_h,threads,chunk for batches (skips the autotuner)")
@@ -415,7 +418,9 @@ def serve_arm(args, ws, rank, local):
     torch.cuda.set_device(local)
     pool = W.config5_pool()
     ctx = capi.Context(local)
-    srv = RenderServer(ctx, budget_bytes=40 << 30, slots=3, max_batch=64, tile=16, threads=64, chunk=64)
+    tw, th, tthreads, tchunk = (int(x) for x in args.serve_tuning.split(","))
+    srv = RenderServer(ctx, budget_bytes=40 << 30, slots=3, max_batch=64, tile=tw, tile_h=th, threads=tthreads,
+                       chunk=tchunk)
     maxpx = 3840 * 2160
     ring = [torch.empty(maxpx * 3, dtype=torch.uint8).pin_memory().numpy() for _ in range(96)]
     ring_ticket = [None] * len(ring)
@@ -445,21 +450,59 @@ def serve_arm(args, ws, rank, local):
 
     stream(W.config5_requests(pool, 64, 1000.0, seed=1))  # warm-up (uploads, allocations)
     rows = []
-    for rate in [float(x) for x in args.rates.split(",")]:
-        reqs = W.config5_requests(pool, args.requests, rate, seed=int(rate))
+    rates = [float(x) for x in args.rates.split(",")]
+    # capacity: every request queued at t = 0 (rate "inf")
+    for rate in rates + [math.inf]:
+        reqs = W.config5_requests(pool, args.requests, rate, seed=_rate_seed(rate))
         srv.reset_stats()
         wall = stream(reqs)
         s = srv.stats()
-        rows.append({"rate_req_s": rate, "frames_per_s": round(s["completed"] / wall, 1),
+        rows.append({"rate_req_s": _rate_label(rate), "frames_per_s": round(s["completed"] / wall, 1),
                      "p50_ms": round(s["p50_us"] / 1e3, 3), "p99_ms": round(s["p99_us"] / 1e3, 3),
                      "max_ms": round(s["max_us"] / 1e3, 3), "mean_batch": round(s["mean_batch"], 2),
                      "requests": int(s["completed"])})
     srv.close()
-    # plain path on the highest-rate sequence: one mr_render + read per request,
-    # new meshes uploaded with mr_mesh_upload, resident meshes kept (LRU by key)
-    rate = float(args.rates.split(",")[-1])
-    reqs = W.config5_requests(pool, args.requests, rate, seed=int(rate))
+    # plain path on the highest-rate sequence and on the capacity sequence: one
+    # mr_render + read per request, new meshes uploaded with mr_mesh_upload,
+    # resident meshes kept (LRU by key)
     from minirender_gb300.renderer import Renderer
+    plain_rows = [plain_stream(args, pool, ring, local, rate) for rate in (rates[-1], math.inf)]
+    ctx.close()
+    served = rows[:-1]
+    cap = rows[-1]
+    best = max(served, key=lambda x: x["frames_per_s"])
+    return {
+        "metric": METRIC, "value": best["frames_per_s"], "unit": UNIT, "n_gpus": ws,
+        "steps": args.requests, "warmup": 64, "ms_per_step": round(1e3 / best["frames_per_s"], 4),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded generator)",
+        "config": {"workload": "Poisson request stream; each request a triangle soup with log-uniform "
+                               "1k-2M triangles at log-uniform 128x128..3840x2160, 30% re-render a "
+                               "resident mesh with a new camera; 40 GB device budget; RGB8 read back",
+                   "server": {"slots": 3, "max_batch": 64,
+                              "tuning": {"tile_w": tw, "tile_h": th, "threads": tthreads, "chunk": tchunk}}},
+        "rates": served, "capacity": cap,
+        "plain_one_frame_per_call": plain_rows[0], "plain_capacity": plain_rows[1],
+        "served_vs_plain_at_max_rate": round(served[-1]["frames_per_s"] / plain_rows[0]["frames_per_s"], 3),
+        "served_vs_plain_capacity": round(cap["frames_per_s"] / plain_rows[1]["frames_per_s"], 3),
+    }
+
+
+def _rate_seed(rate: float) -> int:
+    return int(rate) if math.isfinite(rate) else 99991
+
+
+def _rate_label(rate: float):
+    return rate if math.isfinite(rate) else "all queued at t=0"
+
+
+def plain_stream(args, pool, ring, local, rate):
+    """The request sequence of `rate` through the plain path, one
+    mr_render + synchronous read per request (arrival times honoured)."""
+    from minirender_gb300 import abi
+    from minirender_gb300 import workloads as W
+    from minirender_gb300.renderer import Renderer
+    reqs = W.config5_requests(pool, args.requests, rate, seed=_rate_seed(rate))
     r = Renderer(local)
     r.outputs = abi.MR_OUT_RGB8
     resident = {}
@@ -478,7 +521,6 @@ def serve_arm(args, ws, rank, local):
                 r.ctx.free_mesh(resident.pop(old))
         if q["mesh"] not in tex_h:
             tex_h[q["mesh"]] = r.ctx.upload_texture(mesh.material.texture)
-        from minirender_gb300 import capi as _c
         rs = (abi.mr_renderable * 1)()
         rs[0].mesh = resident[q["key"]]
         rs[0].transform[:] = [float(x) for x in np.eye(4, dtype=np.float32).reshape(16)]
@@ -495,24 +537,12 @@ def serve_arm(args, ws, rank, local):
         done_t.append(time.perf_counter() - t0)
     wall = time.perf_counter() - t0
     lat = np.array(done_t) - np.array([q["t"] for q in reqs])
-    plain = {"rate_req_s": rate, "frames_per_s": round(len(reqs) / wall, 1),
-             "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
-             "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)}
+    for h in resident.values():
+        r.ctx.free_mesh(h)
     r.close()
-    ctx.close()
-    best = max(rows, key=lambda x: x["frames_per_s"])
-    return {
-        "metric": METRIC, "value": best["frames_per_s"], "unit": UNIT, "n_gpus": ws,
-        "steps": args.requests, "warmup": 64, "ms_per_step": round(1e3 / best["frames_per_s"], 4),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded generator)",
-        "config": {"workload": "Poisson request stream; each request a triangle soup with log-uniform "
-                               "1k-2M triangles at log-uniform 128x128..3840x2160, 30% re-render a "
-                               "resident mesh with a new camera; 40 GB device budget; RGB8 read back",
-                   "server": {"slots": 3, "max_batch": 64}},
-        "rates": rows, "plain_one_frame_per_call": plain,
-        "served_vs_plain_at_max_rate": round(rows[-1]["frames_per_s"] / plain["frames_per_s"], 3),
-    }
+    return {"rate_req_s": _rate_label(rate), "frames_per_s": round(len(reqs) / wall, 1),
+            "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+            "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)}
 
 
 def gpu_arm(args, ws, rank, local):
@@ -543,8 +573,17 @@ def gpu_arm(args, ws, rank, local):
         r.ctx.render(frame, rs, n, r.outputs)
         r.ctx.stats()
     r.ctx.synchronize()
+    # per-stage device times: a separate pass with events between the kernels
     r.ctx.set_profiling(True)
     stage_tot = np.zeros(len(STAGES))
+    n_prof = min(args.steps, 10)
+    for _ in range(n_prof):
+        flush.zero_()
+        r.ctx.render(frame, rs, n, r.outputs)
+        s = r.ctx.stats()  # waits for the frame, reads per-stage event times
+        stage_tot += np.array(s.stage_ms[:len(STAGES)], np.float64)
+    stats = r.ctx.stats()
+    r.ctx.set_profiling(False)
     clocks = Clocks(local)
     barrier(ws)
     torch.cuda.synchronize()
@@ -557,16 +596,13 @@ def gpu_arm(args, ws, rank, local):
         e0.record(stream)
         r.ctx.render(frame, rs, n, r.outputs)
         e1.record(stream)
-        s = r.ctx.stats()  # waits for the frame, reads per-stage event times
-        stage_tot += np.array(s.stage_ms[:len(STAGES)], np.float64)
+        r.ctx.stats()  # waits for the frame (and checks its status)
         step_ms.append(e0.elapsed_time(e1))
     torch.cuda.synchronize()
     clk = clocks.stop()
     barrier(ws)
     total_s = max_over_ranks(sum(step_ms) / 1e3, ws)
     value = args.steps * ws / total_s
-    stats = r.ctx.stats()
-    r.ctx.set_profiling(False)
 
     # ---- end to end through the C ABI, host buffers, copies inside the region
     from minirender_gb300 import scene as S
@@ -577,13 +613,16 @@ def gpu_arm(args, ws, rank, local):
         e2e_value, res_value, h2d, d2h = e2e_legs(args, ws, r, sc, st, flat, frame, rs, n,
                                                   mesh_bytes, tex_bytes)
     # ---- roofline of the dominant kernel
-    stage_ms = stage_tot / args.steps
+    stage_ms = stage_tot / n_prof
     dom = int(np.argmax(stage_ms))
     name = STAGES[dom]
     tex_px = P if flat.textures else 0
     n_big = int(stats.binned)
+    # the library runs the per-vertex pass only when vertices are shared
+    # (3T >= 2V); otherwise the setup reads and transforms corners itself
+    vertex_pass = 3 * T >= 2 * V
     alg = {
-        "clear+vertex": 8 * P + 12 * V + 24 * V + 16 * V,
+        "clear+vertex": 8 * P + (12 * V + 24 * V + 16 * V if vertex_pass else 0),
         "setup": 12 * T + 12 * V + 64 * n_big,
         "bin": 2 * 64 * n_big + 8 * int(stats.bin_entries),
         "tile_raster": 64 * int(stats.bin_entries),
@@ -592,7 +631,7 @@ def gpu_arm(args, ws, rank, local):
     peak, peak_kind = peaks()
     achieved = alg[name] / (stage_ms[dom] / 1e3) / 1e9
     traffic = ncu_traffic(args.workload).get(KERNELS[name])
-    frame_bytes = 32 * V + 36 * T + 16 * P + 7 * P + 3 * tex_px
+    frame_bytes = (32 * V if vertex_pass else 12 * V) + 36 * T + 16 * P + 7 * P + 3 * tex_px
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup,
@@ -620,7 +659,8 @@ def gpu_arm(args, ws, rank, local):
         "counters": {"clipped": int(stats.clipped), "rasterised": int(stats.rasterised),
                      "small_direct": int(stats.small_direct), "binned": int(stats.binned),
                      "bin_entries": int(stats.bin_entries)},
-        "gpu_launches": 7 * args.steps,
+        # k_clear, [k_vertex], k_setup, k_bin_tile, k_resolve per frame
+        "gpu_launches": (5 if vertex_pass else 4) * args.steps,
         "clocks": clk,
     }
     if args.views > 0 and not args.no_e2e:

@@ -438,9 +438,15 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   if (c->bins.cap < ((size_t)1 << 20)) CK(c->bins.ensure((size_t)1 << 20), "bin buffer");
   CK(c->rs.ensure(nrs), "renderable table");
   CK(c->tri_base.ensure(3 * (nrs + 1)), "base tables");
-  CK(c->va.ensure(vbase), "vertex buffer");
-  CK(c->vb.ensure(vbase), "vertex buffer");
-  CK(c->vn.ensure(nbase), "normal buffer");
+  // The per-vertex pass pays off when vertices are shared (each one used by
+  // two or more triangle corners on average); for triangle soups every
+  // corner is its own vertex and the kernels transform corners themselves.
+  const bool vertex_pass = 3 * (uint64_t)total >= 2 * (uint64_t)vbase;
+  if (vertex_pass) {
+    CK(c->va.ensure(vbase), "vertex buffer");
+    CK(c->vb.ensure(vbase), "vertex buffer");
+    CK(c->vn.ensure(nbase), "normal buffer");
+  }
   CK(cudaMemcpyAsync(c->rs.p, c->h_rs, sizeof(DevRenderable) * n, cudaMemcpyHostToDevice, c->stream), "renderable upload");
   CK(cudaMemcpyAsync(c->tri_base.p, c->h_tri_base, sizeof(uint32_t) * 3 * (n + 1), cudaMemcpyHostToDevice, c->stream), "base upload");
   CK(cudaMemcpyAsync(c->dP.p, f->projection, sizeof(float) * 16, cudaMemcpyHostToDevice, c->stream), "projection upload");
@@ -476,9 +482,9 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   F.g.nrm_base = c->tri_base.p + 2 * (n + 1);
   F.g.n_verts = (uint32_t)vbase;
   F.g.n_nrms = (uint32_t)nbase;
-  F.g.va = c->va.p;
-  F.g.vb = c->vb.p;
-  F.g.vn = c->vn.p;
+  F.g.va = vertex_pass ? c->va.p : nullptr;  // null: kernels transform per corner
+  F.g.vb = vertex_pass ? c->vb.p : nullptr;
+  F.g.vn = vertex_pass ? c->vn.p : nullptr;
   F.vis = c->vis.p;
   F.recs = c->recs.p;
   F.rec_cap = (uint32_t)std::min<size_t>(c->recs.cap, 0xFFFFFFFFu);

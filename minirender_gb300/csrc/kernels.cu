@@ -745,7 +745,7 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
 
 // Deferred resolve + shade: one thread per pixel.
 template <bool PRE>
-__global__ void __launch_bounds__(256) k_resolve(FrameParams F) {
+__global__ void __launch_bounds__(256, 4) k_resolve(FrameParams F) {
   // loadPPM's texel decode b/255.0f (src/io.cpp:410), one division per byte value
   __shared__ float s_dec[256];
   s_dec[threadIdx.x] = (float)threadIdx.x / 255.0f;
