@@ -51,11 +51,12 @@ def parse():
     p.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4", "config5"])
     p.add_argument("--rates", default="100,500,1000,2000,5000", help="request rates swept (config5)")
     p.add_argument("--requests", type=int, default=1500, help="requests per rate (config5)")
-    p.add_argument("--serve-tuning", default="16,16,64,64",
-                   help="tile_w,tile_h,threads,chunk of the render server's batches (config5)")
+    p.add_argument("--serve-tuning", default="16,16,64,64,64",
+                   help="tile_w,tile_h,threads,chunk,small_max of the render server's batches (config5)")
     p.add_argument("--scenes", type=int, default=256, help="scenes per batch (config4)")
     p.add_argument("--tuning", default="",
-                   help="tile,threads,chunk or tile_w,tile_h,threads,chunk for batches (skips the autotuner)")
+                   help="tile,threads,chunk or tile_w,tile_h,threads,chunk[,small_max] for batches "
+                        "(skips the autotuner)")
     p.add_argument("--views", type=int, default=8, help="camera views per batched launch (config1-3)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs (profiling runs)")
@@ -199,7 +200,7 @@ def cpu_frames_per_s(st, sc, n_threads: int, frames: int):
 
 
 STAGES = ["clear+vertex", "setup", "bin", "tile_raster", "resolve"]
-TUNING_KEYS = ("tile_w", "tile_h", "threads", "chunk")
+TUNING_KEYS = ("tile_w", "tile_h", "threads", "chunk", "small_max")
 KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "bin": "k_bin_count+k_scan+k_bin_scatter",
            "tile_raster": "k_tile_raster", "resolve": "k_resolve"}
 
@@ -325,7 +326,10 @@ def batch_arm(args, ws, rank, local):
         tun = [int(x) for x in args.tuning.split(",")]
         if len(tun) == 3:
             tun = [tun[0]] + tun
-        best = {"tile_w": tun[0], "tile_h": tun[1], "threads": tun[2], "chunk": tun[3], "table": None}
+        if len(tun) == 4:
+            tun.append(autotune.DEFAULT_SMALL_MAX)
+        best = {"tile_w": tun[0], "tile_h": tun[1], "threads": tun[2], "chunk": tun[3], "small_max": tun[4],
+                "table": None}
         autotune.apply(br.ctx, best)
     else:
         best = autotune.tune(br.ctx, prep, autotune.batch_class(len(items), T, P))
@@ -418,9 +422,9 @@ def serve_arm(args, ws, rank, local):
     torch.cuda.set_device(local)
     pool = W.config5_pool()
     ctx = capi.Context(local)
-    tw, th, tthreads, tchunk = (int(x) for x in args.serve_tuning.split(","))
+    tw, th, tthreads, tchunk, tsmall = (int(x) for x in args.serve_tuning.split(","))
     srv = RenderServer(ctx, budget_bytes=40 << 30, slots=3, max_batch=64, tile=tw, tile_h=th, threads=tthreads,
-                       chunk=tchunk)
+                       chunk=tchunk, small_max=tsmall)
     maxpx = 3840 * 2160
     ring = [torch.empty(maxpx * 3, dtype=torch.uint8).pin_memory().numpy() for _ in range(96)]
     ring_ticket = [None] * len(ring)
@@ -448,7 +452,10 @@ def serve_arm(args, ws, rank, local):
                 ring_ticket[k] = None
         return time.perf_counter() - t0
 
-    stream(W.config5_requests(pool, 64, 1000.0, seed=1))  # warm-up (uploads, allocations)
+    # warm-up: a paced stream, then a burst that forms the largest batches, so
+    # every slot's buffers have grown and the memory pools are primed
+    stream(W.config5_requests(pool, 64, 1000.0, seed=1))
+    stream(W.config5_requests(pool, 384, math.inf, seed=2))
     rows = []
     rates = [float(x) for x in args.rates.split(",")]
     # capacity: every request queued at t = 0 (rate "inf")
@@ -480,7 +487,8 @@ def serve_arm(args, ws, rank, local):
                                "1k-2M triangles at log-uniform 128x128..3840x2160, 30% re-render a "
                                "resident mesh with a new camera; 40 GB device budget; RGB8 read back",
                    "server": {"slots": 3, "max_batch": 64,
-                              "tuning": {"tile_w": tw, "tile_h": th, "threads": tthreads, "chunk": tchunk}}},
+                              "tuning": {"tile_w": tw, "tile_h": th, "threads": tthreads, "chunk": tchunk,
+                                         "small_max": tsmall}}},
         "rates": served, "capacity": cap,
         "plain_one_frame_per_call": plain_rows[0], "plain_capacity": plain_rows[1],
         "served_vs_plain_at_max_rate": round(served[-1]["frames_per_s"] / plain_rows[0]["frames_per_s"], 3),

@@ -217,6 +217,11 @@ MR_API int mr_set_batch_tuning(mr_ctx* ctx, int tile, int threads, int chunk);
  * width 4..256, height 2..32, 64..1024 pixels.  Wide tiles shorten the
  * column-by-column edge-function replay of triangles that cross tiles. */
 MR_API int mr_set_batch_tiling(mr_ctx* ctx, int tile_w, int tile_h, int threads, int chunk);
+/* Sub-triangles whose bounding box holds at most small_max pixels (0..4096,
+ * default 64) are rasterised by the batch's setup kernel into a per-scene
+ * visibility buffer; larger ones are binned into the fused tile kernel.
+ * 0: every sub-triangle is binned (no visibility buffer is allocated). */
+MR_API int mr_set_batch_small_max(mr_ctx* ctx, int small_max);
 /* graphs != 0: the launch sequence is captured once per batch shape (scene
  * count, sizes, renderable and triangle counts, tuning) into a CUDA graph and
  * replayed; cameras, lights and materials may change between replays. */
@@ -247,6 +252,7 @@ typedef struct mr_server_opts {
     int32_t max_batch;       /* requests per batch (>= 1) */
     int32_t tile, threads, chunk;   /* batch tuning, as mr_set_batch_tuning (0: defaults) */
     int32_t tile_h;          /* tile height; 0: square tiles of edge `tile` (as mr_set_batch_tiling) */
+    int32_t small_max;       /* as mr_set_batch_small_max; negative: the default (64) */
 } mr_server_opts;
 
 typedef struct mr_request {

@@ -82,7 +82,8 @@ class mr_batch_scene(C.Structure):
 
 class mr_server_opts(C.Structure):
     _fields_ = [("budget_bytes", C.c_uint64), ("slots", C.c_int32), ("max_batch", C.c_int32),
-                ("tile", C.c_int32), ("threads", C.c_int32), ("chunk", C.c_int32), ("tile_h", C.c_int32)]
+                ("tile", C.c_int32), ("threads", C.c_int32), ("chunk", C.c_int32), ("tile_h", C.c_int32),
+                ("small_max", C.c_int32)]
 
 
 class mr_request(C.Structure):

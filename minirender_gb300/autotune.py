@@ -2,9 +2,11 @@
 height), the threads per tile block and the number of records staged per
 shared-memory pass of the persistent fused kernel by timing every candidate
 on the caller's own batch (device time of the vertex, setup and fused
-stages, CUDA-graph replay), and caches the winner in a JSON file keyed by
-GPU name and a coarse class of the batch (scene count, triangle count and
-pixel count, each bucketed by powers of two).
+stages, CUDA-graph replay), then, for the best of those, the bounding-box
+size up to which triangles are rasterised by the setup kernel instead of
+being binned; and caches the winner in a JSON file keyed by GPU name and a
+coarse class of the batch (scene count, triangle count and pixel count, each
+bucketed by powers of two).
 
 Every candidate produces the same pixels; only the work split changes."""
 from __future__ import annotations
@@ -23,9 +25,15 @@ CANDIDATES: List[Tuple[int, int, int, int]] = [(tw, th, t, ch) for tw, th in SHA
                                                for ch in (32, 64, 128)]
 
 
+# bounding-box pixels up to which the setup kernel rasterises (0: bin all)
+SMALL_MAX: List[int] = [0, 16, 64, 256]
+DEFAULT_SMALL_MAX = 64
+
+
 def apply(ctx: capi.Context, best: Dict) -> None:
     """Sets a tuning returned by tune() (or read from its cache)."""
     ctx.set_batch_tiling(best["tile_w"], best["tile_h"], best["threads"], best["chunk"])
+    ctx.set_batch_small_max(best.get("small_max", DEFAULT_SMALL_MAX))
 
 
 def cache_path() -> str:
@@ -54,9 +62,10 @@ def _load(path: str) -> Dict:
         return {}
 
 
-def _time_candidate(ctx: capi.Context, prepared, cand, repeats: int) -> float:
+def _time_candidate(ctx: capi.Context, prepared, cand, repeats: int, small_max: int) -> float:
     scenes, ns, rs, nr = prepared
     ctx.set_batch_tiling(*cand)
+    ctx.set_batch_small_max(small_max)
     ctx.render_batch(scenes, ns, rs, nr)   # captures this shape's graph
     ctx.batch_stats()
     best = float("inf")
@@ -74,7 +83,7 @@ def tune(ctx: capi.Context, prepared, key: str, candidates: Sequence[Tuple[int, 
     Returns {"tile_w", "tile_h", "threads", "chunk", "ms", "table"}."""
     path = path or cache_path()
     cache = _load(path)
-    if not force and key in cache and "tile_w" in cache[key]:
+    if not force and key in cache and "small_max" in cache[key]:
         best = cache[key]
         apply(ctx, best)
         return best
@@ -84,15 +93,23 @@ def tune(ctx: capi.Context, prepared, key: str, candidates: Sequence[Tuple[int, 
     try:
         for cand in candidates:
             try:
-                ms = _time_candidate(ctx, prepared, cand, repeats)
+                ms = _time_candidate(ctx, prepared, cand, repeats, DEFAULT_SMALL_MAX)
             except capi.MRError:
                 continue  # shape does not fit (shared memory / registers)
             table.append({"tile_w": cand[0], "tile_h": cand[1], "threads": cand[2], "chunk": cand[3],
-                          "ms": round(ms, 4)})
+                          "small_max": DEFAULT_SMALL_MAX, "ms": round(ms, 4)})
+        if not table:
+            raise RuntimeError("no batch tuning candidate could run")
+        top = min(table, key=lambda r: r["ms"])
+        cand = (top["tile_w"], top["tile_h"], top["threads"], top["chunk"])
+        for sm in SMALL_MAX:
+            if sm == DEFAULT_SMALL_MAX:
+                continue
+            ms = _time_candidate(ctx, prepared, cand, repeats, sm)
+            table.append({"tile_w": cand[0], "tile_h": cand[1], "threads": cand[2], "chunk": cand[3],
+                          "small_max": sm, "ms": round(ms, 4)})
     finally:
         ctx.set_profiling(False)
-    if not table:
-        raise RuntimeError("no batch tuning candidate could run")
     best = dict(min(table, key=lambda r: r["ms"]))
     best["table"] = table
     apply(ctx, best)

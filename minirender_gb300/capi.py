@@ -46,6 +46,7 @@ _SIGS = {
                            C.POINTER(abi.mr_material), _P, _I, _I, _I, _P, _P, _P, _P], C.c_int),
     "mr_set_batch_tuning": ([_P, C.c_int, C.c_int, C.c_int], C.c_int),
     "mr_set_batch_tiling": ([_P, C.c_int, C.c_int, C.c_int, C.c_int], C.c_int),
+    "mr_set_batch_small_max": ([_P, C.c_int], C.c_int),
     "mr_set_batch_graphs": ([_P, C.c_int], C.c_int),
     "mr_render_batch": ([_P, _P, _I, _P, _I, _I], C.c_int),
     "mr_read_batch": ([_P, _I, _P, _P, _P], C.c_int),
@@ -216,6 +217,9 @@ class Context:
 
     def set_batch_tiling(self, tile_w: int, tile_h: int, threads: int, chunk: int):
         self._check(lib().mr_set_batch_tiling(self.h, tile_w, tile_h, threads, chunk), "mr_set_batch_tiling")
+
+    def set_batch_small_max(self, small_max: int):
+        self._check(lib().mr_set_batch_small_max(self.h, small_max), "mr_set_batch_small_max")
 
     def set_batch_graphs(self, on: bool):
         self._check(lib().mr_set_batch_graphs(self.h, int(on)), "mr_set_batch_graphs")

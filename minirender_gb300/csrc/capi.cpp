@@ -657,6 +657,14 @@ MR_API int mr_set_batch_tiling(mr_ctx* c, int tile_w, int tile_h, int threads, i
   return MR_OK;
 }
 
+MR_API int mr_set_batch_small_max(mr_ctx* c, int small_max) {
+  if (!c) return MR_E_INVALID;
+  if (small_max < 0 || small_max > 4096) return fail(c, MR_E_INVALID, "small_max must be in 0..4096");
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  c->b.small_max = small_max;
+  return MR_OK;
+}
+
 MR_API int mr_set_batch_tuning(mr_ctx* c, int tile, int threads, int chunk) {
   if (!c) return MR_E_INVALID;
   if (tile != 8 && tile != 16 && tile != 32) return fail(c, MR_E_INVALID, "tile must be 8, 16 or 32");
@@ -688,7 +696,7 @@ static int enqueue_batch(mr_ctx* c, BatchSlot& B, cudaStream_t st, cudaEvent_t* 
 int batch_run(mr_ctx* c, BatchSlot& B, cudaStream_t st, bool profiling, cudaEvent_t* ev) {
   std::vector<uint64_t> key = {(uint64_t)B.n_scenes, (uint64_t)B.n_rs, B.P.g.n_tris, B.P.g.n_verts, B.P.g.n_nrms,
                                (uint64_t)B.tile_w, (uint64_t)B.tile_h, (uint64_t)B.threads, (uint64_t)B.chunk,
-                               (uint64_t)B.grid,
+                               (uint64_t)B.grid, (uint64_t)B.P.small_max, (uint64_t)(uintptr_t)B.P.vis,
                                (uint64_t)profiling, (uint64_t)(uintptr_t)st,
                                (uint64_t)(uintptr_t)B.h_rs, (uint64_t)(uintptr_t)B.h_u32,
                                (uint64_t)(uintptr_t)B.h_scenes, (uint64_t)(uintptr_t)B.rs.p,
@@ -736,7 +744,7 @@ int batch_run(mr_ctx* c, BatchSlot& B, cudaStream_t st, bool profiling, cudaEven
 void BatchSlot::release() {
   rs.release(); bases.release(); scenes.release(); stb.release(); va.release(); vn.release();
   vb.release(); recs.release(); rec_scene.release(); tiles.release(); bins.release();
-  block_sums.release(); out8.release(); outd.release(); outi.release();
+  block_sums.release(); out8.release(); outd.release(); outi.release(); vis.release();
   if (h_rs) cudaFreeHost(h_rs);
   if (h_u32) cudaFreeHost(h_u32);
   if (h_scenes) cudaFreeHost(h_scenes);
@@ -812,15 +820,20 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   CK(B.rs.ensure((size_t)n_rs), "batch renderables");
   CK(B.bases.ensure((size_t)3 * (n_rs + 1) + n_scenes + 1), "batch bases");
   CK(B.scenes.ensure((size_t)n_scenes), "batch scenes");
-  CK(B.va.ensure(verts), "batch vertex buffer");
-  CK(B.vb.ensure(verts), "batch vertex buffer");
-  CK(B.vn.ensure(nrms), "batch normal buffer");
+  // per-vertex pass only when vertices are shared (see mr_render)
+  const bool vertex_pass = 3 * tris >= 2 * verts;
+  if (vertex_pass) {
+    CK(B.va.ensure(verts), "batch vertex buffer");
+    CK(B.vb.ensure(verts), "batch vertex buffer");
+    CK(B.vn.ensure(nrms), "batch normal buffer");
+  }
   CK(B.recs.ensure(2 * tris), "batch records");
   CK(B.rec_scene.ensure(2 * tris), "batch records");
   CK(B.tiles.ensure(3 * tiles + 1), "batch tiles");
+  if (B.small_max > 0) CK(B.vis.ensure(pixels), "batch visibility");
   if (B.bins.cap < std::max<size_t>((size_t)1 << 20, 2 * tris))
     CK(B.bins.ensure(std::max<size_t>((size_t)1 << 20, 2 * tris)), "batch bins");
-  int grid = batch_grid(TW, TH, B.chunk, B.threads);
+  int grid = batch_grid(TW, TH, B.chunk, B.threads, vertex_pass);
   if (grid <= 0) return fail(c, MR_E_INVALID, "batch tuning does not fit on the device");
   CK(B.block_sums.ensure((size_t)grid + 1), "batch scan");
   uint32_t tri = 0, vb = 0, nb = 0, tile_base = 0;
@@ -839,6 +852,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
     SR.rgb8 = (outputs & MR_OUT_RGB8) ? B.out8.p + 3 * B.px_off[s] : nullptr;
     SR.depth = (outputs & MR_OUT_DEPTH) ? B.outd.p + B.px_off[s] : nullptr;
     SR.ids = (outputs & MR_OUT_TRI_ID) ? B.outi.p + B.px_off[s] : nullptr;
+    SR.vis = B.small_max > 0 ? B.vis.p + B.px_off[s] : nullptr;
     for (int32_t i = sc[s].first_renderable; i < sc[s].first_renderable + sc[s].n_renderables; i++) {
       const MeshRec& m = c->meshes[rs[i].mesh];
       DevRenderable& R = B.h_rs[i];
@@ -889,9 +903,9 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   P.g.n_tris = tri;
   P.g.n_verts = vb;
   P.g.n_nrms = nb;
-  P.g.va = B.va.p;
-  P.g.vb = B.vb.p;
-  P.g.vn = B.vn.p;
+  P.g.va = vertex_pass ? B.va.p : nullptr;
+  P.g.vb = vertex_pass ? B.vb.p : nullptr;
+  P.g.vn = vertex_pass ? B.vn.p : nullptr;
   P.scenes = B.scenes.p;
   P.scene_tile_base = B.bases.p + 3 * (n_rs + 1);
   P.n_scenes = n_scenes;
@@ -899,6 +913,9 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   P.tile_w = TW;
   P.tile_h = TH;
   P.chunk = B.chunk;
+  P.small_max = B.small_max;
+  P.vis = B.small_max > 0 ? B.vis.p : nullptr;
+  P.n_px = (size_t)pixels;
   P.recs = B.recs.p;
   P.rec_cap = (uint32_t)std::min<size_t>(B.recs.cap, 0xFFFFFFFFu);
   P.rec_scene = B.rec_scene.p;

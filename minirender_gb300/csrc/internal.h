@@ -20,7 +20,7 @@ cudaError_t launch_range(int W, int H, const float* dP, const float* depth, floa
                          cudaStream_t st);
 cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
                          cudaEvent_t* ev);
-int batch_grid(int tile_w, int tile_h, int chunk, int threads);
+int batch_grid(int tile_w, int tile_h, int chunk, int threads, bool pre);
 // Tile shapes k_batch takes: power-of-two sides, 64..1024 pixels (whole warps).
 inline bool batch_tile_ok(int tw, int th) {
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
@@ -82,6 +82,7 @@ using namespace mrgi;
 // one for mr_render_batch; a render server owns several.
 struct BatchSlot {
   int tile_w = 16, tile_h = 16, threads = 256, chunk = 64;
+  int small_max = 64;  // bbox pixels up to which the setup kernel rasterises (0: every triangle binned)
   bool graphs = true;
   DevBuf<DevRenderable> rs;
   DevBuf<uint32_t> bases;
@@ -91,6 +92,7 @@ struct BatchSlot {
   DevBuf<float2> vb;
   DevBuf<BigRec> recs;
   DevBuf<uint32_t> rec_scene, tiles, bins, block_sums;
+  DevBuf<unsigned long long> vis;
   DevBuf<uint8_t> out8;
   DevBuf<float> outd;
   DevBuf<uint32_t> outi;

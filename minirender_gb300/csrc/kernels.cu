@@ -408,6 +408,36 @@ __device__ __forceinline__ void winner_zterms(const View& V, const Geo& G, const
   }
 }
 
+// The setup (src/Renderer.cpp:198-224) of the winning sub-triangle, the same
+// values its raster used.
+template <bool PRE>
+__device__ __forceinline__ void winner_setup(const View& V, const Geo& G, const DevRenderable& R,
+                                             const int (&ip)[3], const Vtx (&vc)[3], bool clipped, Setup& S) {
+  if (PRE && !clipped) {
+    V2 p[3];
+    float zt[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      float4 a = G.va[R.vert_base + ip[c]];
+      p[c] = v2(a.x, a.y);
+      zt[c] = a.z;
+    }
+    setup_from(V, p, zt, S);
+  } else {
+    setup_view(V, vc, S);
+  }
+}
+
+// The running edge values at pixel (x, y): row start, then column by column
+// from the bounding-box edge (src/Renderer.cpp:240-243).
+__device__ __forceinline__ void replay(const Setup& S, int x, int y, float& e1, float& e2) {
+  row_start(S, y, e1, e2);
+  for (int c = S.x0; c < x; c++) {
+    e1 += S.n1.x;
+    e2 += S.n2.x;
+  }
+}
+
 // Shading of the pixel (x, y) whose visibility word is vw, src/Renderer.cpp:
 // 247-305 (FAST_LIGHT): re-derives the winner's setup, replays its edge
 // functions to column x, and evaluates texture and Blinn-Phong lighting.
@@ -429,27 +459,9 @@ __device__ __forceinline__ void resolve_pixel(const View& V, const Geo& G, int r
   bool clipped;
   const DevRenderable& R = *winner_tri<PRE>(V, G, rs_lo, rs_hi, id, ip, vc, clipped);
   Setup S;
-  if (clipped) {
-    setup_view(V, vc, S);
-  } else if (PRE) {
-    V2 p[3];
-    float zt[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      float4 a = G.va[R.vert_base + ip[c]];
-      p[c] = v2(a.x, a.y);
-      zt[c] = a.z;
-    }
-    setup_from(V, p, zt, S);
-  } else {
-    setup_view(V, vc, S);
-  }
+  winner_setup<PRE>(V, G, R, ip, vc, clipped, S);
   float e1, e2;
-  row_start(S, y, e1, e2);
-  for (int c = S.x0; c < x; c++) {
-    e1 += S.n1.x;
-    e2 += S.n2.x;
-  }
+  replay(S, x, y, e1, e2);
   float k0, k1, k2;
   depth = frag_depth(S, V.persp != 0, e1, e2, k0, k1, k2);
   shade(V, R, vc, k0, k1, k2, s_dec, value, normal_out);
@@ -507,10 +519,110 @@ struct __align__(16) SmallRec {
   float p0x, p0y, p2x, p2y, n1x, n1y, n2x, n2y, z0, z1, z2;
   uint32_t id;
   int x0, y0, x1, rows;
+  uint32_t tag;  // target frame (batches: scene)
 };
 
 constexpr int kSetupThreads = 256;
 constexpr int kSetupWarps = kSetupThreads / 32;
+
+// Where small triangles' fragments go: the frame's visibility buffer...
+struct FrameTarget {
+  unsigned long long* vis;
+  int W;
+  bool persp;
+  __device__ unsigned long long* row(uint32_t, int y) const { return vis + (size_t)y * W; }
+  __device__ bool perspective(uint32_t) const { return persp; }
+};
+// ...or, in a batch, the visibility buffer of the triangle's scene (tag).
+struct BatchTarget {
+  const SceneRec* scenes;
+  __device__ unsigned long long* row(uint32_t sc, int y) const {
+    return scenes[sc].vis + (size_t)y * scenes[sc].v.W;
+  }
+  __device__ bool perspective(uint32_t sc) const { return scenes[sc].v.persp != 0; }
+};
+
+// Raster of the warp's small sub-triangles (kind 1) of triangle g, whose
+// frame is `tag`, with 64-bit atomicMin into the target (src/Renderer.cpp:
+// 238-269).  When every one in the warp spans at most 4x4 pixels the lanes
+// rasterise their own (the loops are short and nearly uniform); otherwise
+// they are staged in shared memory and rasterised with one (triangle, row)
+// per lane so every lane has work.  Called by all lanes of the warp.
+template <class Target>
+__device__ __forceinline__ void raster_small(const Setup (&S)[2], const int (&kind)[2], uint32_t g, uint32_t tag,
+                                             const Target& T, SmallRec* s_rec, int* s_pre) {
+  const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+  int span = 0;
+#pragma unroll
+  for (int s = 0; s < 2; s++)
+    if (kind[s] == 1) span = max(span, max(S[s].x1 - S[s].x0, S[s].y1 - S[s].y0) + 1);
+  if (__reduce_max_sync(0xffffffffu, (unsigned)span) <= 4u) {
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+      if (kind[s] == 1) {
+        const uint32_t id = 2u * g + (uint32_t)s;
+        const bool persp = T.perspective(tag);
+        for (int y = S[s].y0; y <= S[s].y1; y++) {
+          unsigned long long* row = T.row(tag, y);
+          walk_row(S[s], persp, id, y, S[s].x0, S[s].x1,
+                   [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
+        }
+      }
+    return;
+  }
+  int n = 0;
+#pragma unroll
+  for (int s = 0; s < 2; s++) {
+    unsigned m = __ballot_sync(0xffffffffu, kind[s] == 1);
+    if (kind[s] == 1) {
+      SmallRec& q = s_rec[n + __popc(m & lt)];
+      q.p0x = S[s].p0.x; q.p0y = S[s].p0.y; q.p2x = S[s].p2.x; q.p2y = S[s].p2.y;
+      q.n1x = S[s].n1.x; q.n1y = S[s].n1.y; q.n2x = S[s].n2.x; q.n2y = S[s].n2.y;
+      q.z0 = S[s].z[0]; q.z1 = S[s].z[1]; q.z2 = S[s].z[2];
+      q.id = 2u * g + (uint32_t)s;
+      q.x0 = S[s].x0; q.y0 = S[s].y0; q.x1 = S[s].x1;
+      q.rows = S[s].y1 - S[s].y0 + 1;
+      q.tag = tag;
+    }
+    n += __popc(m);
+  }
+  __syncwarp();
+  if (n == 0) return;
+  int c0 = (int)lane < n ? s_rec[lane].rows : 0;
+  int c1 = (int)lane + 32 < n ? s_rec[lane + 32].rows : 0;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int u0 = __shfl_up_sync(0xffffffffu, c0, o), u1 = __shfl_up_sync(0xffffffffu, c1, o);
+    if ((int)lane >= o) { c0 += u0; c1 += u1; }
+  }
+  int tot0 = __shfl_sync(0xffffffffu, c0, 31), tot1 = __shfl_sync(0xffffffffu, c1, 31);
+  if (lane == 0) s_pre[0] = 0;
+  s_pre[lane + 1] = c0;
+  s_pre[lane + 33] = tot0 + c1;
+  __syncwarp();
+  const int total = tot0 + tot1;
+  for (int b = 0; b < total; b += 32) {
+    int k = b + (int)lane;
+    if (k < total) {
+      int lo = 0, hi = n;
+      while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (s_pre[mid] <= k) lo = mid; else hi = mid;
+      }
+      const SmallRec& q = s_rec[lo];
+      Setup U;
+      U.p0 = v2(q.p0x, q.p0y); U.p2 = v2(q.p2x, q.p2y);
+      U.n1 = v2(q.n1x, q.n1y); U.n2 = v2(q.n2x, q.n2y);
+      U.z[0] = q.z0; U.z[1] = q.z1; U.z[2] = q.z2;
+      U.x0 = q.x0; U.x1 = q.x1; U.y0 = q.y0;
+      const int y = q.y0 + (k - s_pre[lo]);
+      unsigned long long* row = T.row(q.tag, y);
+      walk_row(U, T.perspective(q.tag), q.id, y, U.x0, U.x1,
+               [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
+    }
+  }
+  __syncwarp();  // s_rec / s_pre free for the warp's next use
+}
 
 template <bool PRE>
 __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
@@ -554,84 +666,7 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
       if (slot < F.rec_cap) F.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
     }
   }
-  bool direct;
-  // Small records.  When every one in the warp spans at most 4x4 pixels the
-  // lanes rasterise their own (the loops are short and nearly uniform);
-  // otherwise they are staged in shared memory and rasterised with one
-  // (triangle, row) per lane so every lane has work.
-  {
-    int span = 0;
-#pragma unroll
-    for (int s = 0; s < 2; s++)
-      if (kind[s] == 1) span = max(span, max(S[s].x1 - S[s].x0, S[s].y1 - S[s].y0) + 1);
-    direct = __reduce_max_sync(0xffffffffu, (unsigned)span) <= 4u;
-    if (direct) {
-      unsigned long long* vis = F.vis;
-      const int W = F.v.W;
-#pragma unroll
-      for (int s = 0; s < 2; s++)
-        if (kind[s] == 1) {
-          const uint32_t id = 2u * g + (uint32_t)s;
-          for (int y = S[s].y0; y <= S[s].y1; y++)
-            walk_row(S[s], persp, id, y, S[s].x0, S[s].x1, [&](int x, unsigned long long v, float, float) {
-              atomicMin(vis + (size_t)y * W + x, v);
-            });
-        }
-    }
-  }
-  int n = 0;
-#pragma unroll
-  for (int s = 0; s < 2; s++) {
-    unsigned m = __ballot_sync(0xffffffffu, kind[s] == 1 && !direct);
-    if (kind[s] == 1 && !direct) {
-      SmallRec& q = s_rec[w][n + __popc(m & lt)];
-      q.p0x = S[s].p0.x; q.p0y = S[s].p0.y; q.p2x = S[s].p2.x; q.p2y = S[s].p2.y;
-      q.n1x = S[s].n1.x; q.n1y = S[s].n1.y; q.n2x = S[s].n2.x; q.n2y = S[s].n2.y;
-      q.z0 = S[s].z[0]; q.z1 = S[s].z[1]; q.z2 = S[s].z[2];
-      q.id = 2u * g + (uint32_t)s;
-      q.x0 = S[s].x0; q.y0 = S[s].y0; q.x1 = S[s].x1;
-      q.rows = S[s].y1 - S[s].y0 + 1;
-    }
-    n += __popc(m);
-  }
-  __syncwarp();
-  if (n > 0) {
-    int c0 = (int)lane < n ? s_rec[w][lane].rows : 0;
-    int c1 = (int)lane + 32 < n ? s_rec[w][lane + 32].rows : 0;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int u0 = __shfl_up_sync(0xffffffffu, c0, o), u1 = __shfl_up_sync(0xffffffffu, c1, o);
-      if ((int)lane >= o) { c0 += u0; c1 += u1; }
-    }
-    int tot0 = __shfl_sync(0xffffffffu, c0, 31), tot1 = __shfl_sync(0xffffffffu, c1, 31);
-    if (lane == 0) s_pre[w][0] = 0;
-    s_pre[w][lane + 1] = c0;
-    s_pre[w][lane + 33] = tot0 + c1;
-    __syncwarp();
-    const int total = tot0 + tot1;
-    unsigned long long* vis = F.vis;
-    const int W = F.v.W;
-    for (int b = 0; b < total; b += 32) {
-      int k = b + (int)lane;
-      if (k < total) {
-        int lo = 0, hi = n;
-        while (hi - lo > 1) {
-          int mid = (lo + hi) >> 1;
-          if (s_pre[w][mid] <= k) lo = mid; else hi = mid;
-        }
-        const SmallRec& q = s_rec[w][lo];
-        Setup T;
-        T.p0 = v2(q.p0x, q.p0y); T.p2 = v2(q.p2x, q.p2y);
-        T.n1 = v2(q.n1x, q.n1y); T.n2 = v2(q.n2x, q.n2y);
-        T.z[0] = q.z0; T.z[1] = q.z1; T.z[2] = q.z2;
-        T.x0 = q.x0; T.x1 = q.x1; T.y0 = q.y0;
-        const int y = q.y0 + (k - s_pre[w][lo]);
-        walk_row(T, persp, q.id, y, T.x0, T.x1, [&](int x, unsigned long long v, float, float) {
-          atomicMin(vis + (size_t)y * W + x, v);
-        });
-      }
-    }
-  }
+  raster_small(S, kind, g, 0u, FrameTarget{F.vis, F.v.W, persp}, s_rec[w], s_pre[w]);
   block_count(bc, 0, n_raster);
   block_count(bc, 1, n_small);
   block_count(bc, 2, n_clipped);
@@ -780,29 +815,39 @@ __global__ void __launch_bounds__(256, 4) k_resolve(FrameParams F) {
 // ---------------------------------------------------------------- batches
 // Setup of every triangle of every scene: each sub-triangle with pixels to
 // test becomes a record (warp-compacted), counted into its scene's tiles.
-__global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
+template <bool PRE>
+__global__ void __launch_bounds__(kSetupThreads) k_setup_batch(BatchParams B) {
+  __shared__ SmallRec s_rec[kSetupWarps][64];
+  __shared__ int s_pre[kSetupWarps][65];
   __shared__ BlockCounters bc;
   __shared__ unsigned s_fill, s_base;
   if (threadIdx.x < 3) bc.v[threadIdx.x] = 0;
   if (threadIdx.x == 0) s_fill = 0;
   __syncthreads();
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
+  const unsigned lane = threadIdx.x & 31, w = threadIdx.x >> 5, lt = (1u << lane) - 1u;
   Setup S[2];
-  int kind[2] = {0, 0};
-  unsigned n_clipped = 0, n_raster = 0;
+  int kind[2] = {0, 0};  // 0 none, 1 small (rasterised here), 2 record
+  unsigned n_clipped = 0, n_raster = 0, n_small = 0;
   uint32_t scene = 0;
   if (g < B.g.n_tris) {
     const DevRenderable& R = B.g.rs[find_base(B.g.tri_base, 0, B.g.n_renderables, g)];
     scene = R.scene;
-    if (!setup_triangle<true>(B.scenes[scene].v, B.g, R, g, S, kind, n_clipped))
+    if (!setup_triangle<PRE>(B.scenes[scene].v, B.g, R, g, S, kind, n_clipped))
       atomicOr(&B.counters->error_flags, 1u);
-    n_raster = (kind[0] != 0) + (kind[1] != 0);
+#pragma unroll
+    for (int s = 0; s < 2; s++)
+      if (kind[s]) {
+        n_raster++;
+        long long bw = S[s].x1 - S[s].x0 + 1, bh = S[s].y1 - S[s].y0 + 1;
+        if (bw * bh <= (long long)B.small_max) n_small++;
+        else kind[s] = 2;
+      }
   }
   // record slots: each warp reserves within the block, the block once globally
   unsigned m2[2], wbase = 0;
 #pragma unroll
-  for (int s = 0; s < 2; s++) m2[s] = __ballot_sync(0xffffffffu, kind[s] != 0);
+  for (int s = 0; s < 2; s++) m2[s] = __ballot_sync(0xffffffffu, kind[s] == 2);
   const unsigned wn = __popc(m2[0]) + __popc(m2[1]);
   if (lane == 0 && wn) wbase = atomicAdd(&s_fill, wn);
   wbase = __shfl_sync(0xffffffffu, wbase, 0);
@@ -814,7 +859,7 @@ __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
   for (int s = 0; s < 2; s++) {
     const unsigned m = m2[s];
     if (m == 0) continue;
-    if (kind[s]) {
+    if (kind[s] == 2) {
       unsigned slot = base + __popc(m & lt);
       if (slot < B.rec_cap) {
         B.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
@@ -828,9 +873,11 @@ __global__ void __launch_bounds__(256) k_setup_batch(BatchParams B) {
     }
     base += __popc(m);
   }
+  if (B.small_max > 0) raster_small(S, kind, g, scene, BatchTarget{B.scenes}, s_rec[w], s_pre[w]);
   block_count(bc, 0, n_raster);
+  block_count(bc, 1, n_small);
   block_count(bc, 2, n_clipped);
-  block_flush(bc, &B.counters->rasterised, nullptr, &B.counters->clipped);
+  block_flush(bc, &B.counters->rasterised, &B.counters->small_direct, &B.counters->clipped);
 }
 
 // Renderables per scene whose triangle bases k_batch keeps in shared memory
@@ -959,7 +1006,7 @@ __device__ __forceinline__ void raster_items(const BigRec* s_recs, const uint32_
 // MINB: blocks of 256 threads per SM the register allocation must allow
 // (2: up to 128 registers per thread, for 64-thread blocks; 4: up to 64, so
 // that 128- and 256-thread blocks keep enough warps resident).
-template <int MINB>
+template <int MINB, bool PRE>
 __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* block_sums) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int TW = B.tile_w, TH = B.tile_h, TP = TW * TH;
@@ -977,6 +1024,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
   __shared__ uint8_t* s_out8;
   __shared__ float* s_outd;
   __shared__ uint32_t* s_outi;
+  __shared__ const unsigned long long* s_invis;  // small triangles' visibility words of the scene
   cg::grid_group grid = cg::this_grid();
   const uint32_t nb = gridDim.x, nt = blockDim.x;
   for (uint32_t i = threadIdx.x; i < 256; i += nt) s_dec[i] = (float)i / 255.0f;
@@ -1066,6 +1114,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
           s_out8 = SR.rgb8;
           s_outd = SR.depth;
           s_outi = SR.ids;
+          s_invis = SR.vis;
         }
       }
       if (lane == 0) s_tile = t;
@@ -1073,7 +1122,6 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
     __syncthreads();
     const uint32_t tile = s_tile;
     if (tile >= B.n_tiles) break;
-    for (int i = threadIdx.x; i < TP; i += nt) svis[i] = VIS_EMPTY;
     const int n_rs = s_meta[4] - s_meta[3];
     const bool tb_shared = n_rs <= kBatchTbMax;
     if (tb_shared && s_tb_scene != s_meta[0]) {  // uniform: read after the barrier above
@@ -1084,6 +1132,14 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
     const int lt = s_meta[1], tx = lt % s_meta[2], ty = lt / s_meta[2];
     const int px0 = tx * TW, py0 = ty * TH;
     const int px1 = min(px0 + TW, s_view.W) - 1, py1 = min(py0 + TH, s_view.H) - 1;
+    // the tile starts from the small triangles' words (or empty); captured
+    // edge values start as NaN (no fragment with a NaN edge value is ever
+    // written: its depth is NaN and fails z < 1e11f)
+    for (int i = threadIdx.x; i < TP; i += nt) {
+      const int x = px0 + i % TW, y = py0 + i / TW;
+      svis[i] = (s_invis && x <= px1 && y <= py1) ? s_invis[(size_t)y * s_view.W + x] : VIS_EMPTY;
+      s_e[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
+    }
     const uint32_t s = (uint32_t)s_meta[6], e = (uint32_t)s_meta[7];
     const bool persp = s_view.persp != 0;
     const uint32_t nck = (e - s + (uint32_t)B.chunk - 1) / (uint32_t)B.chunk;
@@ -1113,13 +1169,21 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
         int ip[3];
         Vtx vc[3];
         bool clipped;
-        const DevRenderable& R = *winner_tri<true>(s_view, B.g, s_meta[3], s_meta[4], id, ip, vc, clipped,
+        const DevRenderable& R = *winner_tri<PRE>(s_view, B.g, s_meta[3], s_meta[4], id, ip, vc, clipped,
                                                    tb_shared ? s_tb : nullptr);
         Setup S;
-        winner_zterms<true>(s_view, B.g, R, ip, vc, clipped, S.z);
+        float e1, e2;
         const float2 ee = s_e[i];
+        if (ee.x == ee.x) {  // won by a record of this tile: edge values captured
+          winner_zterms<PRE>(s_view, B.g, R, ip, vc, clipped, S.z);
+          e1 = ee.x;
+          e2 = ee.y;
+        } else {  // won by a small triangle rasterised in the setup kernel
+          winner_setup<PRE>(s_view, B.g, R, ip, vc, clipped, S);
+          replay(S, x, y, e1, e2);
+        }
         float k0, k1, k2;
-        depth = frag_depth(S, persp, ee.x, ee.y, k0, k1, k2);
+        depth = frag_depth(S, persp, e1, e2, k0, k1, k2);
         shade(s_view, R, vc, k0, k1, k2, s_dec, value, normal);
       }
       const size_t px = (size_t)y * s_view.W + x;
@@ -1234,14 +1298,15 @@ size_t batch_smem(int tile_w, int tile_h, int chunk) {
   return (size_t)tile_w * tile_h * (sizeof(unsigned long long) + sizeof(float2)) + (size_t)chunk * sizeof(BigRec) +
          (size_t)(chunk + 1) * sizeof(uint32_t);
 }
-static const void* batch_kernel(int threads) {
-  return threads <= 64 ? (const void*)k_batch<2> : (const void*)k_batch<4>;
+static const void* batch_kernel(int threads, bool pre) {
+  if (pre) return threads <= 64 ? (const void*)k_batch<2, true> : (const void*)k_batch<4, true>;
+  return threads <= 64 ? (const void*)k_batch<2, false> : (const void*)k_batch<4, false>;
 }
 // Co-resident blocks of k_batch for the given shape (its cooperative grid).
-int batch_grid(int tile_w, int tile_h, int chunk, int threads) {
+int batch_grid(int tile_w, int tile_h, int chunk, int threads, bool pre) {
   int per = 0;
   size_t smem = batch_smem(tile_w, tile_h, chunk);
-  const void* k = batch_kernel(threads);
+  const void* k = batch_kernel(threads, pre);
   cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, threads, smem);
   if (per <= 0) return 0;
@@ -1249,17 +1314,25 @@ int batch_grid(int tile_w, int tile_h, int chunk, int threads) {
 }
 cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
                          cudaEvent_t* ev) {
+  const bool pre = B.g.va != nullptr;  // null: kernels transform corners themselves
   if (ev) cudaEventRecord(ev[0], st);
-  if (B.g.n_verts + B.g.n_nrms > 0) {
+  if (pre && B.g.n_verts + B.g.n_nrms > 0) {
     View none = {};
     k_vertex<<<grid_for((size_t)B.g.n_verts + B.g.n_nrms, 256), 256, 0, st>>>(B.g, none, B.scenes);
   }
+  if (B.small_max > 0 && B.n_px) {  // small triangles' visibility words of every scene
+    int cgrid = grid_for(B.n_px, 256);
+    k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(B.vis, B.n_px);
+  }
   if (ev) cudaEventRecord(ev[1], st);
-  if (B.g.n_tris) k_setup_batch<<<grid_for(B.g.n_tris, 256), 256, 0, st>>>(B);
+  if (B.g.n_tris) {
+    if (pre) k_setup_batch<true><<<grid_for(B.g.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(B);
+    else k_setup_batch<false><<<grid_for(B.g.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(B);
+  }
   if (ev) cudaEventRecord(ev[2], st);
   BatchParams Bc = B;
   void* args[] = {&Bc, &block_sums};
-  cudaError_t e = launch_coop(batch_kernel(threads), grid, threads, args, batch_smem(B.tile_w, B.tile_h, B.chunk),
+  cudaError_t e = launch_coop(batch_kernel(threads, pre), grid, threads, args, batch_smem(B.tile_w, B.tile_h, B.chunk),
                               st);
   if (ev) cudaEventRecord(ev[3], st);
   if (e != cudaSuccess) return e;

@@ -122,6 +122,7 @@ struct SceneRec {
   uint8_t* rgb8;
   float* depth;
   uint32_t* ids;
+  unsigned long long* vis;    // visibility words of the small triangles (null: all binned)
 };
 
 // Batched launch: many scenes, one persistent fused bin-raster-shade kernel.
@@ -132,6 +133,9 @@ struct BatchParams {
   int n_scenes;
   uint32_t n_tiles;
   int tile_w, tile_h, chunk;        // tile width and height (pixels), records staged per pass
+  int small_max;                    // bbox pixels up to which the setup kernel rasterises (0: none)
+  unsigned long long* vis;          // all scenes' visibility words (small_max > 0)
+  size_t n_px;                      // pixels of all scenes
   BigRec* recs;
   uint32_t rec_cap;
   uint32_t* rec_scene;              // scene of each record

@@ -326,7 +326,9 @@ MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out)
   if (!c || !o || !out || o->slots < 1 || o->max_batch < 1 || o->budget_bytes == 0) return MR_E_INVALID;
   const int tw = o->tile ? o->tile : 16, th = o->tile_h ? o->tile_h : tw;
   const int threads = o->threads ? o->threads : 64, chunk = o->chunk ? o->chunk : 64;
-  if (!batch_tile_ok(tw, th) || (threads != 64 && threads != 128 && threads != 256) || chunk < 16 || chunk > 256)
+  const int small_max = o->small_max < 0 ? 64 : o->small_max;
+  if (!batch_tile_ok(tw, th) || (threads != 64 && threads != 128 && threads != 256) || chunk < 16 || chunk > 256 ||
+      small_max > 4096)
     return MR_E_INVALID;
   mr_server* s = new mr_server();
   s->c = c;
@@ -338,6 +340,7 @@ MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out)
     sl->b.tile_h = th;
     sl->b.threads = threads;
     sl->b.chunk = chunk;
+    sl->b.small_max = small_max;
     sl->b.graphs = false;  // shapes change from batch to batch
     if (cudaStreamCreateWithFlags(&sl->stream, cudaStreamNonBlocking) != cudaSuccess) {
       delete sl;

@@ -16,11 +16,13 @@ from .scene import Material, TriMesh
 
 class RenderServer:
     def __init__(self, ctx: capi.Context, budget_bytes: int = 40 << 30, slots: int = 2, max_batch: int = 32,
-                 tile: int = 16, threads: int = 64, chunk: int = 64, tile_h: int = 0):
+                 tile: int = 16, threads: int = 64, chunk: int = 64, tile_h: int = 0, small_max: int = -1):
         """tile x tile_h screen tiles (tile_h 0: square), threads per tile
-        block and records per shared-memory pass of the fused batch kernel."""
+        block and records per shared-memory pass of the fused batch kernel;
+        small_max: bbox pixels up to which the setup kernel rasterises
+        (negative: the library default)."""
         self.ctx = ctx
-        o = abi.mr_server_opts(budget_bytes, slots, max_batch, tile, threads, chunk, tile_h)
+        o = abi.mr_server_opts(budget_bytes, slots, max_batch, tile, threads, chunk, tile_h, small_max)
         h = C.c_void_p()
         rc = capi.lib().mr_server_create(ctx.h, C.byref(o), C.byref(h))
         if rc != 0:

@@ -90,11 +90,28 @@ def test_batch_rectangular_tiles_same_result(batch, refs, tw, th, threads, chunk
         batch.ctx.set_batch_tuning(16, 256, 64)
 
 
+@pytest.mark.parametrize("small_max", [0, 16, 4096])
+def test_batch_small_max_same_result(batch, refs, small_max):
+    """Triangles rasterised by the setup kernel (bbox <= small_max pixels)
+    and triangles binned into the fused tile kernel give the same pixels."""
+    batch.ctx.set_batch_graphs(True)
+    batch.ctx.set_batch_tuning(16, 128, 64)
+    batch.ctx.set_batch_small_max(small_max)
+    try:
+        _check_all(batch, _items(), refs, f"s{small_max}")
+    finally:
+        batch.ctx.set_batch_small_max(64)
+        batch.ctx.set_batch_tuning(16, 256, 64)
+
+
 def test_batch_tiling_rejects_bad_shapes(batch):
     from minirender_gb300 import capi
     for bad in [(48, 16, 64, 64), (512, 2, 64, 64), (8, 4, 64, 64), (64, 32, 64, 64), (16, 16, 96, 64)]:
         with pytest.raises(capi.MRError):
             batch.ctx.set_batch_tiling(*bad)
+    for bad in (-1, 4097):
+        with pytest.raises(capi.MRError):
+            batch.ctx.set_batch_small_max(bad)
 
 
 @pytest.mark.parametrize("tile,threads,chunk", [(8, 64, 16), (16, 128, 256), (32, 256, 32), (32, 128, 128)])
@@ -105,3 +122,18 @@ def test_batch_tuning_same_result(batch, refs, tile, threads, chunk):
         _check_all(batch, _items(), refs, f"t{tile}_{threads}_{chunk}")
     finally:
         batch.ctx.set_batch_tuning(16, 256, 64)
+
+
+def test_batch_of_triangle_soups(batch):
+    """Soups (no shared vertices: the kernels transform corners themselves,
+    no per-vertex pass) with exact duplicate triangles, small and binned."""
+    items = [W.config3(n_tris=20000, width=320, height=240, seed=70 + k) for k in range(3)]
+    items.append(W.config3(n_tris=3000, width=640, height=360, seed=77))
+    refs = [O.render(st, sc) for st, sc in items]
+    batch.ctx.set_batch_graphs(True)
+    try:
+        for small_max in (64, 0):
+            batch.ctx.set_batch_small_max(small_max)
+            _check_all(batch, items, refs, f"soup{small_max}")
+    finally:
+        batch.ctx.set_batch_small_max(64)
