@@ -421,6 +421,10 @@ def serve_arm(args, ws, rank, local):
     from minirender_gb300.server import RenderServer
     torch.cuda.set_device(local)
     pool = W.config5_pool()
+    # the asset store lives in page-locked host memory (uploads are DMA, the
+    # same for the server and the plain path)
+    for m in pool:
+        _pin_mesh(m)
     ctx = capi.Context(local)
     tw, th, tthreads, tchunk, tsmall = (int(x) for x in args.serve_tuning.split(","))
     srv = RenderServer(ctx, budget_bytes=40 << 30, slots=3, max_batch=64, tile=tw, tile_h=th, threads=tthreads,
@@ -454,13 +458,14 @@ def serve_arm(args, ws, rank, local):
 
     # warm-up: a paced stream, then a burst that forms the largest batches, so
     # every slot's buffers have grown and the memory pools are primed
-    stream(W.config5_requests(pool, 64, 1000.0, seed=1))
-    stream(W.config5_requests(pool, 384, math.inf, seed=2))
+    keys = iter(range(1, 1 << 40, 1 << 20))  # a fresh key range per stream
+    stream(W.config5_requests(pool, 64, 1000.0, seed=1, key_base=next(keys)))
+    stream(W.config5_requests(pool, 384, math.inf, seed=2, key_base=next(keys)))
     rows = []
     rates = [float(x) for x in args.rates.split(",")]
     # capacity: every request queued at t = 0 (rate "inf")
     for rate in rates + [math.inf]:
-        reqs = W.config5_requests(pool, args.requests, rate, seed=_rate_seed(rate))
+        reqs = W.config5_requests(pool, args.requests, rate, seed=_rate_seed(rate), key_base=next(keys))
         srv.reset_stats()
         wall = stream(reqs)
         s = srv.stats()
@@ -494,6 +499,23 @@ def serve_arm(args, ws, rank, local):
         "served_vs_plain_at_max_rate": round(served[-1]["frames_per_s"] / plain_rows[0]["frames_per_s"], 3),
         "served_vs_plain_capacity": round(cap["frames_per_s"] / plain_rows[1]["frames_per_s"], 3),
     }
+
+
+def _pin_mesh(mesh) -> None:
+    """Moves a TriMesh's arrays into page-locked host memory (in place)."""
+    import torch
+    pinned = {}
+    keep = []
+    for name in ("vertices", "normals", "indices", "normalsI", "texcoords", "texcoordsI"):
+        a = getattr(mesh, name)
+        if id(a) not in pinned:
+            t = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory()
+            b = t.numpy().view(a.dtype).reshape(a.shape)
+            b[...] = a
+            keep.append(t)
+            pinned[id(a)] = b
+        setattr(mesh, name, pinned[id(a)])
+    mesh._pinned = keep
 
 
 def _rate_seed(rate: float) -> int:

@@ -447,16 +447,17 @@ def config5_pool(n_meshes: int = 24, seed: int = 5, t_min: int = 1000, t_max: in
     return pool
 
 
-def config5_requests(pool, n: int, rate: float, seed: int = 7, rerender: float = 0.3):
+def config5_requests(pool, n: int, rate: float, seed: int = 7, rerender: float = 0.3, key_base: int = 1):
     """A Poisson request stream: arrival times (s), resolution log-uniform
     from 128x128 to 3840x2160, a fresh mesh key (the mesh must be uploaded)
     or, with probability `rerender`, a recently used key re-rendered from a
-    new camera."""
+    new camera.  Fresh keys count up from key_base (give each stream its own
+    range so that no key of an earlier stream is found resident)."""
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate, n))
     out = []
     recent: List[Tuple[int, int]] = []
-    next_key = 1
+    next_key = key_base
     for i in range(n):
         u = rng.uniform()
         w = int(round(128 * (3840 / 128) ** u))
