@@ -181,13 +181,48 @@ def ncu_traffic(workload: str):
         return json.load(f).get(workload, {})
 
 
+_MESH_ARRAYS = ("vertices", "normals", "indices", "normalsI", "texcoords", "texcoordsI")
+
+
+def _mesh_upload_bytes(m) -> int:
+    """Bytes a mesh upload copies: index arrays given as the indices array
+    itself are shared on the device, not copied again."""
+    seen = {}
+    for name in _MESH_ARRAYS:
+        a = getattr(m, name)
+        if a.size and name in ("texcoordsI",) and not m.texcoords.size:
+            continue
+        seen.setdefault((a.ctypes.data, a.nbytes), a.nbytes)
+    return sum(seen.values())
+
+
+def _pinned_copy(m):
+    """The TriMesh's arrays copied into page-locked host memory, arrays that
+    share memory (normalsI / texcoordsI given as the indices) still shared.
+    Returns (mesh with the pinned arrays as attributes, tensors to keep)."""
+    import copy
+    import torch
+    out = copy.copy(m)
+    pinned, keep = {}, []
+    for name in _MESH_ARRAYS:
+        a = getattr(m, name)
+        k = (a.ctypes.data, a.nbytes, a.dtype.str, a.shape)
+        if k not in pinned:
+            t = torch.empty(max(1, a.nbytes), dtype=torch.uint8).pin_memory()
+            b = t[:a.nbytes].numpy().view(a.dtype).reshape(a.shape)
+            b[...] = a
+            keep.append(t)
+            pinned[k] = b
+        setattr(out, name, pinned[k])
+    return out, keep
+
+
 def scene_sizes(sc):
     from minirender_gb300 import scene as S
     flat = S.flatten(sc)
     V = sum(m.vertices.shape[0] for m in flat.meshes)
     T = sum(m.n_triangles for m in flat.meshes)
-    mesh_bytes = sum(m.vertices.nbytes + m.normals.nbytes + m.texcoords.nbytes + 3 * m.indices.nbytes
-                     for m in flat.meshes)
+    mesh_bytes = sum(_mesh_upload_bytes(m) for m in flat.meshes)
     tex_bytes = sum(t.nbytes for t in flat.textures)
     return V, T, mesh_bytes, tex_bytes
 
@@ -213,9 +248,7 @@ def e2e_legs(args, ws, r, sc, st, flat, frame, rs, n, mesh_bytes, tex_bytes):
     from minirender_gb300 import scene as S
     mesh = flat.meshes[0]
     pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
-    pm = S.TriMesh(pin(mesh.vertices), pin(mesh.normals), pin(mesh.indices), normalsI=pin(mesh.normalsI),
-                   texcoords=pin(mesh.texcoords) if mesh.texcoords.size else None,
-                   texcoordsI=pin(mesh.texcoordsI) if mesh.texcoordsI.size else None)
+    pm, _keep = _pinned_copy(mesh)
     ptex = [pin(t) for t in flat.textures]
     mh = r._mesh_handle(mesh)
     th = [r._texture_handle(t) for t in flat.textures]
@@ -503,18 +536,9 @@ def serve_arm(args, ws, rank, local):
 
 def _pin_mesh(mesh) -> None:
     """Moves a TriMesh's arrays into page-locked host memory (in place)."""
-    import torch
-    pinned = {}
-    keep = []
-    for name in ("vertices", "normals", "indices", "normalsI", "texcoords", "texcoordsI"):
-        a = getattr(mesh, name)
-        if id(a) not in pinned:
-            t = torch.empty(a.nbytes, dtype=torch.uint8).pin_memory()
-            b = t.numpy().view(a.dtype).reshape(a.shape)
-            b[...] = a
-            keep.append(t)
-            pinned[id(a)] = b
-        setattr(mesh, name, pinned[id(a)])
+    pm, keep = _pinned_copy(mesh)
+    for name in _MESH_ARRAYS:
+        setattr(mesh, name, getattr(pm, name))
     mesh._pinned = keep
 
 

@@ -132,17 +132,23 @@ static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t 
   M.pos = (const float*)take((size_t)12 * d->n_vertices);
   M.nrm = (const float*)take((size_t)12 * d->n_normals);
   M.uv = (const float*)take((size_t)8 * (M.has_uv ? d->n_texcoords : 0));
+  // normalsI / texcoordsI given as the very array of indices (the usual case:
+  // one index per corner for every attribute) share its device copy; the
+  // kernels then reuse the corner's vertex index
+  const bool n_alias = d->normalsI == d->indices, t_alias = M.has_uv && d->texcoordsI == d->indices;
   M.idx = (const int32_t*)take((size_t)4 * d->n_indices);
-  M.nidx = (const int32_t*)take((size_t)4 * d->n_indices);
-  M.tidx = (const int32_t*)take((size_t)4 * (M.has_uv ? d->n_indices : 0));
+  M.nidx = n_alias ? M.idx : (const int32_t*)take((size_t)4 * d->n_indices);
+  M.tidx = t_alias ? M.idx : (const int32_t*)take((size_t)4 * (M.has_uv ? d->n_indices : 0));
   M.bad = (const uint32_t*)take((size_t)4 * ((M.n_tri + 31) / 32 + 1));
   if (d->n_vertices) CK(cudaMemcpyAsync((void*)M.pos, d->vertices, (size_t)12 * d->n_vertices, cudaMemcpyHostToDevice, st), "mesh copy");
   if (d->n_normals) CK(cudaMemcpyAsync((void*)M.nrm, d->normals, (size_t)12 * d->n_normals, cudaMemcpyHostToDevice, st), "mesh copy");
   if (M.has_uv) CK(cudaMemcpyAsync((void*)M.uv, d->texcoords, (size_t)8 * d->n_texcoords, cudaMemcpyHostToDevice, st), "mesh copy");
   if (d->n_indices) {
     CK(cudaMemcpyAsync((void*)M.idx, d->indices, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
-    CK(cudaMemcpyAsync((void*)M.nidx, d->normalsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
-    if (M.has_uv) CK(cudaMemcpyAsync((void*)M.tidx, d->texcoordsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
+    if (!n_alias)
+      CK(cudaMemcpyAsync((void*)M.nidx, d->normalsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
+    if (M.has_uv && !t_alias)
+      CK(cudaMemcpyAsync((void*)M.tidx, d->texcoordsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
   }
   CK(launch_validate(M, (uint32_t*)M.bad, st), "validate launch");
   return MR_OK;
@@ -166,9 +172,12 @@ static int check_desc(mr_ctx* c, const mr_mesh_desc* d) {
 
 static size_t mesh_bytes(const mr_mesh_desc* d, bool has_uv) {
   int ntri = d->n_indices / 3;
+  const bool n_alias = d->normalsI == d->indices, t_alias = has_uv && d->texcoordsI == d->indices;
   return align256((size_t)12 * d->n_vertices) + align256((size_t)12 * d->n_normals) +
-         align256((size_t)8 * (has_uv ? d->n_texcoords : 0)) + 2 * align256((size_t)4 * d->n_indices) +
-         align256((size_t)4 * (has_uv ? d->n_indices : 0)) + align256((size_t)4 * ((ntri + 31) / 32 + 1));
+         align256((size_t)8 * (has_uv ? d->n_texcoords : 0)) + align256((size_t)4 * d->n_indices) +
+         (n_alias ? 0 : align256((size_t)4 * d->n_indices)) +
+         (t_alias ? 0 : align256((size_t)4 * (has_uv ? d->n_indices : 0))) +
+         align256((size_t)4 * ((ntri + 31) / 32 + 1));
 }
 
 int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes) {
@@ -239,6 +248,9 @@ MR_API int mr_mesh_update(mr_ctx* c, int32_t h, const mr_mesh_desc* d) {
   if (d->n_vertices != m.d.n_pos || d->n_normals != m.d.n_nrm || d->n_indices != m.n_idx ||
       has_uv != (m.d.has_uv != 0) || (has_uv && d->n_texcoords != m.d.n_uv))
     return fail(c, MR_E_INVALID, "mr_mesh_update needs the same element counts");
+  if ((d->normalsI == d->indices) != (m.d.nidx == m.d.idx) ||
+      (has_uv && (d->texcoordsI == d->indices) != (m.d.tidx == m.d.idx)))
+    return fail(c, MR_E_INVALID, "mr_mesh_update needs normalsI / texcoordsI shared with indices as at upload");
   cudaSetDevice(c->device);
   return copy_mesh(c, m, d, c->stream);
 }

@@ -131,14 +131,17 @@ __device__ __forceinline__ void corners(const Geo& G, const DevRenderable& R, in
       v[c].pos = affine(R.mv, ld3(M.pos, ip[c]));
     }
     if (ATTR) {
-      int in = __ldg(M.nidx + 3 * t + c);
+      // normalsI / texcoordsI shared with the indices: reuse the corner's index
+      // (PRE only: without the vertex pass the extra live registers spill,
+      // and the shared words are L1-hot anyway)
+      const int in = (PRE && M.nidx == M.idx) ? ip[c] : __ldg(M.nidx + 3 * t + c);
       if (PRE) {
         float4 n = G.vn[R.nrm_base + in];
         v[c].nrm = v3(n.x, n.y, n.z);
       } else {
         v[c].nrm = affine(R.nm, ld3(M.nrm, in));
       }
-      v[c].uv = M.has_uv ? ld2(M.uv, __ldg(M.tidx + 3 * t + c)) : v2(0, 0);
+      v[c].uv = M.has_uv ? ld2(M.uv, (PRE && M.tidx == M.idx) ? ip[c] : __ldg(M.tidx + 3 * t + c)) : v2(0, 0);
     }
   }
 }

@@ -62,11 +62,12 @@ size_t mesh_footprint(const mr_mesh_desc& d) {
 }
 
 // Device bytes a request occupies while it runs: its outputs and the
-// per-triangle, per-vertex and per-tile working buffers of a batch.
+// per-triangle, per-vertex, per-pixel (visibility words) and per-tile
+// working buffers of a batch.
 size_t request_footprint(const mr_request& r) {
   const size_t px = (size_t)r.frame.width * r.frame.height;
   const size_t nt = (size_t)(r.mesh.n_indices / 3);
-  size_t out = 0;
+  size_t out = 8 * px;
   if (r.outputs & MR_OUT_RGB8) out += 3 * px;
   if (r.outputs & MR_OUT_DEPTH) out += 4 * px;
   if (r.outputs & MR_OUT_TRI_ID) out += 4 * px;

@@ -86,3 +86,30 @@ def test_deterministic(renderer):
     b, _ = gpu_render(st, sc, renderer)
     for k in ("ids", "depth", "rgb8", "image"):
         assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
+
+
+def test_shared_and_separate_index_arrays(renderer):
+    """normalsI / texcoordsI passed as the indices array itself share its
+    device copy; passed as equal but separate arrays they are copied: same
+    pixels either way.  An update must keep the sharing of the upload."""
+    from minirender_gb300 import capi
+    from minirender_gb300.scene import Scene, TriMesh
+    st, sc = W.config2(level=5, width=320, height=240, tex_size=64)
+    m = sc.children[0]
+    assert m.normalsI.ctypes.data == m.indices.ctypes.data == m.texcoordsI.ctypes.data
+    sep = TriMesh(m.vertices, m.normals, m.indices, normalsI=m.indices.copy(), texcoords=m.texcoords,
+                  texcoordsI=m.indices.copy(), material=m.material)
+    sc2 = Scene()
+    sc2.add(sep)
+    a, _ = gpu_render(st, sc, renderer)
+    b, _ = gpu_render(st, sc2, renderer)
+    for k in ("ids", "depth", "rgb8"):
+        assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), k
+    ctx = renderer.ctx
+    h = ctx.upload_mesh(m.desc())
+    try:
+        with pytest.raises(capi.MRError):
+            ctx.update_mesh(h, sep.desc())
+        ctx.update_mesh(h, m.desc())
+    finally:
+        ctx.free_mesh(h)
