@@ -781,17 +781,23 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
   }
 }
 
-// Deferred resolve + shade: one thread per pixel.
+// Deferred resolve + shade: one thread per pixel, 256-thread blocks over
+// 32x8-pixel tiles.
+constexpr int kResolveTileW = 32, kResolveTileH = 8;
 template <bool PRE>
 __global__ void __launch_bounds__(256, 4) k_resolve(FrameParams F) {
   // loadPPM's texel decode b/255.0f (src/io.cpp:410), one division per byte value
   __shared__ float s_dec[256];
   s_dec[threadIdx.x] = (float)threadIdx.x / 255.0f;
   __syncthreads();
-  size_t px = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t npx = (size_t)F.v.W * F.v.H;
-  if (px >= npx) return;
-  const int y = (int)(px / F.v.W), x = (int)(px - (size_t)y * F.v.W);
+  // 32x8-pixel block tiles, 16x2 per warp: neighbouring rows of a small
+  // triangle are shaded by the same warp, so its corner data is fetched once
+  const int tiles_x = (F.v.W + kResolveTileW - 1) / kResolveTileW;
+  const int bx = blockIdx.x % tiles_x, by = blockIdx.x / tiles_x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int x = bx * kResolveTileW + (lane & 15) + 16 * (w & 1), y = by * kResolveTileH + (lane >> 4) + 2 * (w >> 1);
+  if (x >= F.v.W || y >= F.v.H) return;
+  const size_t px = (size_t)y * F.v.W + x;
   V3 value, normal;
   float depth;
   uint32_t id;
@@ -1290,8 +1296,9 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   }
   if (ev) cudaEventRecord(ev[3], st);
   if (ev) cudaEventRecord(ev[4], st);
-  if (pre) k_resolve<true><<<grid_for(npx, 256), 256, 0, st>>>(F);
-  else k_resolve<false><<<grid_for(npx, 256), 256, 0, st>>>(F);
+  const int rgrid = ((F.v.W + kResolveTileW - 1) / kResolveTileW) * ((F.v.H + kResolveTileH - 1) / kResolveTileH);
+  if (pre) k_resolve<true><<<rgrid, 256, 0, st>>>(F);
+  else k_resolve<false><<<rgrid, 256, 0, st>>>(F);
   if (ev) cudaEventRecord(ev[5], st);
   return cudaGetLastError();
 }
