@@ -236,8 +236,11 @@ def cpu_frames_per_s(st, sc, n_threads: int, frames: int):
 
 STAGES = ["clear+vertex", "setup", "bin", "tile_raster", "resolve"]
 TUNING_KEYS = ("tile_w", "tile_h", "threads", "chunk", "small_max")
-KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "bin": "k_bin_count+k_scan+k_bin_scatter",
-           "tile_raster": "k_tile_raster", "resolve": "k_resolve"}
+# kernels between the stage events of one plain frame (the binning and tile
+# raster of large triangles are one cooperative kernel; "tile_raster" is the
+# empty interval after it)
+KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "bin": "k_bin_tile",
+           "tile_raster": "k_bin_tile", "resolve": "k_resolve"}
 
 
 def e2e_legs(args, ws, r, sc, st, flat, frame, rs, n, mesh_bytes, tex_bytes):

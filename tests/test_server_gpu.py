@@ -123,3 +123,24 @@ def test_server_budget_admission_and_eviction(ctx):
         assert srv.stats()["committed_bytes"] <= 64 << 20
     finally:
         srv.close()
+
+
+def test_server_other_tunings_same_result(ctx):
+    """Every request equals the oracle whatever the server's batch tuning:
+    all triangles binned (small_max 0), wide tiles, bigger blocks."""
+    from minirender_gb300.server import RenderServer
+    pool = _pool()[:4]
+    refs = [_oracle(st, m) for st, m in pool]
+    for opts in (dict(small_max=0), dict(tile=64, tile_h=16, threads=128, chunk=128, small_max=256)):
+        srv = RenderServer(ctx, budget_bytes=8 << 30, slots=2, max_batch=8, **opts)
+        try:
+            tickets = []
+            for rep in range(2):
+                for i, (st, m) in enumerate(pool):
+                    out = _buffers(st)
+                    tickets.append((i, out, srv.submit(st, m, mesh_key=300 + i, texture_key=700 + i, out=out)))
+            for i, out, t in tickets:
+                assert srv.wait(t).status == 0
+                assert _same(out, refs[i]), f"request {i} differs with {opts}"
+        finally:
+            srv.close()
