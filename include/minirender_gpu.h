@@ -48,6 +48,7 @@ extern "C" {
 #define MR_E_NOT_READY -8    /* asynchronous result not available yet */
 #define MR_E_NO_DEVICE -9    /* no usable CUDA device */
 #define MR_E_NOALLOC_LIMIT -10 /* frame or mesh larger than mr_render_noalloc's fixed scratch */
+#define MR_E_IO -11          /* a file could not be read, written or parsed */
 
 /* Background sentinel in the per-pixel triangle-id image. */
 #define MR_NO_TRIANGLE 0xFFFFFFFFu
@@ -330,6 +331,34 @@ MR_API int mr_render_noalloc(const mr_frame* frame, const mr_mesh_desc* mesh, co
                              const mr_material* material, const void* texture, int32_t tex_rows,
                              int32_t tex_cols, int32_t tex_is_rgb8, uint8_t* rgb8, float* depth,
                              uint32_t* tri_id, void* cuda_stream);
+
+/* ---- model and image files (host only, no device work) -------------------
+ * loadMesh (src/io.cpp:111-132) for .stl (loadSTL :134-153, ASCII :16-60 or
+ * binary :62-109), .obj (+ .mtl, loadOBJ :187-335) and .x3d (src/x3d.cpp:
+ * 35-200); any other extension gives an empty node, as the reference does.
+ * The model is the scene tree the reference builds: mr_node array in
+ * pre-order (node 0 the returned node; a TriMesh without material has
+ * has_material 0; material.texture indexes the model's textures), one
+ * mr_mesh_desc per TriMesh (host arrays owned by the model), RGB8 textures
+ * read with loadPPM's rules (:364-415; decode b/255.0f happens on the
+ * device).  Large OBJ and binary STL files are parsed on all host threads. */
+typedef struct mr_model mr_model;
+MR_API int mr_model_load(const char* path, mr_model** out);
+MR_API int mr_model_counts(const mr_model* model, int32_t* n_nodes, int32_t* n_meshes, int32_t* n_textures);
+MR_API int mr_model_nodes(const mr_model* model, mr_node* out, int32_t cap);
+MR_API int mr_model_mesh(const mr_model* model, int32_t mesh, mr_mesh_desc* out);
+MR_API int mr_model_texture(const mr_model* model, int32_t texture, const uint8_t** rgb8, int32_t* rows,
+                            int32_t* cols);
+MR_API void mr_model_free(mr_model* model);
+/* loadPPM (src/io.cpp:364-415) as bytes: rows/cols always, pixels when rgb8
+ * is given and cap_bytes >= rows*cols*3. */
+MR_API int mr_ppm_load(const char* path, uint8_t* rgb8, int64_t cap_bytes, int32_t* rows, int32_t* cols);
+/* savePPM (src/io.cpp:337-362) of an RGB8 image (mr_read's bytes are already
+ * quantised as savePPM does). */
+MR_API int mr_ppm_save(const char* path, const uint8_t* rgb8, int32_t rows, int32_t cols);
+/* saveSTL (src/io.cpp:155-183): binary STL of the mesh's triangles under a
+ * row-major transform (NULL: identity). */
+MR_API int mr_stl_save(const char* path, const mr_mesh_desc* mesh, const float* transform);
 
 /* ---- host helpers (no device work) -------------------------------------- */
 /* Scene::collectShapes (src/Scene.cpp:13-36) over a pre-order node array.

@@ -16,6 +16,7 @@ MR_E_TIMEOUT = -7
 MR_E_NOT_READY = -8
 MR_E_NO_DEVICE = -9
 MR_E_NOALLOC_LIMIT = -10
+MR_E_IO = -11
 MR_NOALLOC_MAX_SIDE = 4096
 MR_NOALLOC_MAX_PIXELS = 1 << 21
 MR_NOALLOC_MAX_TRIANGLES = 1 << 22

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libminirender_gpu.so")
-SOURCES = ["kernels.cu", "capi.cpp", "host_math.cpp", "noalloc.cu", "server.cpp"]
+SOURCES = ["kernels.cu", "capi.cpp", "host_math.cpp", "noalloc.cu", "server.cpp", "loaders.cpp"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 # -fmad=false / IEEE division and sqrt / no flush-to-zero on the device, and

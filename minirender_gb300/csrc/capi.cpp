@@ -26,6 +26,7 @@ MR_API const char* mr_status_string(int s) {
     case MR_E_NOT_READY: return "not ready";
     case MR_E_NO_DEVICE: return "no CUDA device";
     case MR_E_NOALLOC_LIMIT: return "request exceeds the fixed scratch of mr_render_noalloc";
+    case MR_E_IO: return "file could not be read, written or parsed";
     default: return "unknown status";
   }
 }

@@ -29,6 +29,16 @@ class Matrix4_ {
   static Matrix4_ translate(const Vec3_<T>& t) { return translate(t.x, t.y, t.z); }
   static Matrix4_ scale(T s) { return Matrix4_(s, 0, 0, 0, 0, s, 0, 0, 0, 0, s, 0, 0, 0, 0, 1); }
   static Matrix4_ scale(T x, T y, T z) { return Matrix4_(x, 0, 0, 0, 0, y, 0, 0, 0, 0, z, 0, 0, 0, 0, 1); }
+  static Matrix4_ scale(const Vec3_<T>& s) { return scale(s.x, s.y, s.z); }
+  // rotation by angle t about the axis a (normalized), right-handed
+  static Matrix4_ rotate(const Vec3_<T>& a, T t) {
+    Vec3_<T> u = a.normalized();
+    T c = cos(t), s = sin(t), k = 1 - c;
+    return Matrix4_(k * u.x * u.x + c, k * u.x * u.y - s * u.z, k * u.x * u.z + s * u.y, 0,
+                    k * u.x * u.y + s * u.z, k * u.y * u.y + c, k * u.y * u.z - s * u.x, 0,
+                    k * u.x * u.z - s * u.y, k * u.y * u.z + s * u.x, k * u.z * u.z + c, 0,
+                    0, 0, 0, 1);
+  }
   static Matrix4_ rotateX(T t) { T c = cos(t), s = sin(t); return Matrix4_(1, 0, 0, 0, 0, c, -s, 0, 0, s, c, 0, 0, 0, 0, 1); }
   static Matrix4_ rotateY(T t) { T c = cos(t), s = sin(t); return Matrix4_(c, 0, s, 0, 0, 1, 0, 0, -s, 0, c, 0, 0, 0, 0, 1); }
   static Matrix4_ rotateZ(T t) { T c = cos(t), s = sin(t); return Matrix4_(c, -s, 0, 0, s, c, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1); }

@@ -90,8 +90,77 @@ def ref_lib() -> Optional[C.CDLL]:
         L.ref_projection.argtypes = [C.c_int, C.c_void_p, C.c_void_p]
         L.ref_mat4_mul.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
         L.ref_mat4_inverse.argtypes = [C.c_void_p, C.c_void_p]
+        L.ref_model_load.restype = C.c_void_p
+        L.ref_model_load.argtypes = [C.c_char_p]
+        L.ref_model_counts.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_model_nodes.argtypes = [C.c_void_p, C.c_void_p]
+        L.ref_model_mesh.argtypes = [C.c_void_p, C.c_int] + [C.c_void_p] * 7
+        L.ref_model_texture.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_model_free.argtypes = [C.c_void_p]
+        L.ref_ppm_load.restype = C.c_int
+        L.ref_ppm_load.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.ref_ppm_save.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]
+        L.ref_stl_save.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p]
         _ref = L
     return _ref
+
+
+def ref_load_mesh(path: str):
+    """The reference's loadMesh(path), flattened: {"nodes": mr_node array in
+    pre-order, "meshes": [dict of arrays], "textures": [(rows, cols, 3) float32]}
+    or None when it returns NULL."""
+    L = ref_lib()
+    h = L.ref_model_load(path.encode())
+    if not h:
+        return None
+    try:
+        nn, nm, nt = C.c_int32(), C.c_int32(), C.c_int32()
+        L.ref_model_counts(h, C.byref(nn), C.byref(nm), C.byref(nt))
+        nodes = (abi.mr_node * max(1, nn.value))()
+        L.ref_model_nodes(h, nodes)
+        meshes = []
+        for i in range(nm.value):
+            cnt = np.zeros(6, np.int32)
+            L.ref_model_mesh(h, i, _ptr(cnt), None, None, None, None, None, None)
+            m = {"vertices": np.zeros((cnt[0], 3), np.float32), "normals": np.zeros((cnt[1], 3), np.float32),
+                 "texcoords": np.zeros((cnt[2], 2), np.float32), "indices": np.zeros(cnt[3], np.int32),
+                 "normalsI": np.zeros(cnt[4], np.int32), "texcoordsI": np.zeros(cnt[5], np.int32)}
+            L.ref_model_mesh(h, i, _ptr(cnt), *[_ptr(m[k]) for k in ("vertices", "normals", "texcoords", "indices",
+                                                                      "normalsI", "texcoordsI")])
+            meshes.append(m)
+        textures = []
+        for i in range(nt.value):
+            r, c = C.c_int32(), C.c_int32()
+            L.ref_model_texture(h, i, C.byref(r), C.byref(c), None)
+            t = np.zeros((r.value, c.value, 3), np.float32)
+            L.ref_model_texture(h, i, C.byref(r), C.byref(c), _ptr(t))
+            textures.append(t)
+        return {"nodes": nodes[:nn.value], "meshes": meshes, "textures": textures}
+    finally:
+        L.ref_model_free(h)
+
+
+def ref_load_ppm(path: str) -> np.ndarray:
+    """The reference's loadPPM: (rows, cols, 3) float32 (empty if unreadable)."""
+    L = ref_lib()
+    r, c = C.c_int32(), C.c_int32()
+    L.ref_ppm_load(path.encode(), C.byref(r), C.byref(c), None)
+    out = np.zeros((r.value, c.value, 3), np.float32)
+    if out.size:
+        L.ref_ppm_load(path.encode(), C.byref(r), C.byref(c), _ptr(out))
+    return out
+
+
+def ref_save_ppm(path: str, rgb: np.ndarray) -> None:
+    """The reference's savePPM of a float image (rows, cols, 3)."""
+    a = np.ascontiguousarray(rgb, np.float32)
+    ref_lib().ref_ppm_save(path.encode(), _ptr(a), a.shape[0], a.shape[1])
+
+
+def ref_save_stl(path: str, desc, transform=None) -> None:
+    """The reference's saveSTL of a mesh (mr_mesh_desc) under transform."""
+    xf = None if transform is None else np.ascontiguousarray(transform, np.float32)
+    ref_lib().ref_stl_save(path.encode(), C.byref(desc), None if xf is None else _ptr(xf))
 
 
 def _ptr(a: np.ndarray):

@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "minirender/Renderer.h"
+#include "minirender/io.h"
 #include "minirender/primitives.h"
 #include "../include/minirender_gpu.h"
 
@@ -178,5 +179,128 @@ void ref_projection(int kind, const float* p, float* out) {
 // Matrix4 product / inverse as the stand-in ASL computes them.
 void ref_mat4_mul(const float* a, const float* b, float* out) { from_m4(to_m4(a) * to_m4(b), out); }
 void ref_mat4_inverse(const float* a, float* out) { from_m4(to_m4(a).inverse(), out); }
+
+// ---- loaders: the reference's loadMesh / loadPPM / savePPM / saveSTL
+// (src/io.cpp, src/x3d.cpp), flattened for comparison.
+struct RefModel {
+  std::vector<mr_node> nodes;
+  std::vector<TriMesh*> meshes;
+  std::vector<const Material*> textures;  // materials with a non-empty texture
+  Shared<SceneNode> root;
+};
+
+static void flatten(RefModel& M, const Shared<SceneNode>& n, int parent) {
+  mr_node nd;
+  memset(&nd, 0, sizeof nd);
+  nd.parent = parent;
+  nd.mesh = -1;
+  from_m4(n->transform, nd.transform);
+  nd.material.texture = -1;
+  if (TriMesh* t = dynamic_cast<TriMesh*>(n.ptr())) {
+    nd.mesh = (int32_t)M.meshes.size();
+    M.meshes.push_back(t);
+    if (t->material) {
+      const Material& m = *t->material;
+      nd.has_material = 1;
+      nd.material.diffuse[0] = m.diffuse.x; nd.material.diffuse[1] = m.diffuse.y; nd.material.diffuse[2] = m.diffuse.z;
+      nd.material.specular[0] = m.specular.x; nd.material.specular[1] = m.specular.y;
+      nd.material.specular[2] = m.specular.z;
+      nd.material.emissive[0] = m.emissive.x; nd.material.emissive[1] = m.emissive.y;
+      nd.material.emissive[2] = m.emissive.z;
+      nd.material.shininess = m.shininess;
+      if (m.texture.rows() > 0) {
+        int id = -1;
+        for (size_t k = 0; k < M.textures.size(); k++)
+          if (M.textures[k] == &m) id = (int)k;
+        if (id < 0) {
+          id = (int)M.textures.size();
+          M.textures.push_back(&m);
+        }
+        nd.material.texture = id;
+      }
+    }
+  }
+  const int self = (int)M.nodes.size();
+  M.nodes.push_back(nd);
+  for (int i = 0; i < n->children.length(); i++) flatten(M, n->children[i], self);
+}
+
+void* ref_model_load(const char* path) {
+  Shared<SceneNode> root = loadMesh(path);
+  if (!root) return nullptr;
+  RefModel* M = new RefModel();
+  M->root = root;
+  flatten(*M, root, -1);
+  return M;
+}
+void ref_model_counts(void* h, int32_t* n_nodes, int32_t* n_meshes, int32_t* n_textures) {
+  RefModel* M = (RefModel*)h;
+  *n_nodes = (int32_t)M->nodes.size();
+  *n_meshes = (int32_t)M->meshes.size();
+  *n_textures = (int32_t)M->textures.size();
+}
+void ref_model_nodes(void* h, mr_node* out) {
+  RefModel* M = (RefModel*)h;
+  memcpy(out, M->nodes.data(), sizeof(mr_node) * M->nodes.size());
+}
+// counts: vertices, normals, texcoords, indices, normalsI, texcoordsI; arrays may be NULL
+void ref_model_mesh(void* h, int i, int32_t* counts, float* vertices, float* normals, float* texcoords,
+                    int32_t* indices, int32_t* normalsI, int32_t* texcoordsI) {
+  TriMesh* m = ((RefModel*)h)->meshes[i];
+  counts[0] = m->vertices.length(); counts[1] = m->normals.length(); counts[2] = m->texcoords.length();
+  counts[3] = m->indices.length(); counts[4] = m->normalsI.length(); counts[5] = m->texcoordsI.length();
+  for (int k = 0; vertices && k < counts[0]; k++) {
+    vertices[3 * k] = m->vertices[k].x; vertices[3 * k + 1] = m->vertices[k].y; vertices[3 * k + 2] = m->vertices[k].z;
+  }
+  for (int k = 0; normals && k < counts[1]; k++) {
+    normals[3 * k] = m->normals[k].x; normals[3 * k + 1] = m->normals[k].y; normals[3 * k + 2] = m->normals[k].z;
+  }
+  for (int k = 0; texcoords && k < counts[2]; k++) {
+    texcoords[2 * k] = m->texcoords[k].x; texcoords[2 * k + 1] = m->texcoords[k].y;
+  }
+  if (indices && counts[3]) memcpy(indices, m->indices.ptr(), sizeof(int32_t) * counts[3]);
+  if (normalsI && counts[4]) memcpy(normalsI, m->normalsI.ptr(), sizeof(int32_t) * counts[4]);
+  if (texcoordsI && counts[5]) memcpy(texcoordsI, m->texcoordsI.ptr(), sizeof(int32_t) * counts[5]);
+}
+// rgb: rows*cols*3 floats (NULL: sizes only)
+void ref_model_texture(void* h, int i, int32_t* rows, int32_t* cols, float* rgb) {
+  const Array2<Vec3>& t = ((RefModel*)h)->textures[i]->texture;
+  *rows = t.rows();
+  *cols = t.cols();
+  for (int r = 0; rgb && r < t.rows(); r++)
+    for (int c = 0; c < t.cols(); c++) {
+      const Vec3& v = t(r, c);
+      float* o = rgb + 3 * ((size_t)r * t.cols() + c);
+      o[0] = v.x; o[1] = v.y; o[2] = v.z;
+    }
+}
+void ref_model_free(void* h) { delete (RefModel*)h; }
+
+// loadPPM: sizes always; floats when rgb is given.  Returns 0 for an empty image.
+int ref_ppm_load(const char* path, int32_t* rows, int32_t* cols, float* rgb) {
+  Array2<Vec3> t = loadPPM(path);
+  *rows = t.rows();
+  *cols = t.cols();
+  for (int r = 0; rgb && r < t.rows(); r++)
+    for (int c = 0; c < t.cols(); c++) {
+      float* o = rgb + 3 * ((size_t)r * t.cols() + c);
+      o[0] = t(r, c).x; o[1] = t(r, c).y; o[2] = t(r, c).z;
+    }
+  return t.rows() > 0;
+}
+void ref_ppm_save(const char* path, const float* rgb, int32_t rows, int32_t cols) {
+  Array2<Vec3> t(rows, cols);
+  for (int r = 0; r < rows; r++)
+    for (int c = 0; c < cols; c++) {
+      const float* v = rgb + 3 * ((size_t)r * cols + c);
+      t(r, c) = Vec3(v[0], v[1], v[2]);
+    }
+  savePPM(t, path);
+}
+void ref_stl_save(const char* path, const mr_mesh_desc* d, const float* transform) {
+  Shared<TriMesh> m = make_mesh(*d);
+  if (transform) m->transform = to_m4(transform);
+  saveSTL(m, path);
+}
 
 }  // extern "C"

@@ -29,9 +29,26 @@ def cases():
         yield "edge_" + name, fn(128, 96) if name == "big_triangles" else fn()
 
 
+def loader_digests():
+    """tests/golden/loaders.json: digests of the reference loaders' output
+    (src/io.cpp, src/x3d.cpp) for the seeded sample files of
+    tests/loader_files.py, serialised as tests/test_loaders_cpu.py does."""
+    import json
+    import tempfile
+
+    import loader_files
+    import test_loaders_cpu as T
+    with tempfile.TemporaryDirectory() as d:
+        out = {n: T.digest(O.ref_load_mesh(os.path.join(d, n))) for n in loader_files.write_all(d)}
+    with open(os.path.join(HERE, "loaders.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("loaders.json:", ", ".join(sorted(out)))
+
+
 def main():
     if O.ref_lib() is None:
         sys.exit("reference sources not available")
+    loader_digests()
     for name, (st, sc) in cases():
         r = O.ref_render(st, sc, normals=st.save_normals)
         expect = {"image": r["image"], "depth": r["depth"]}

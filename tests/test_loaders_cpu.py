@@ -1,0 +1,206 @@
+"""The library's model and image file loaders (host code, no GPU) against the
+reference's own loadMesh / loadSTL / loadOBJ / X3D reader / loadPPM /
+savePPM / saveSTL (src/io.cpp, src/x3d.cpp built as the checker): the same
+scene tree, bit-identical arrays and materials, identical written files.
+Without the reference build the same models are checked against digests of
+the reference's output (tests/golden/loaders.json, tests/golden/make_golden.py)."""
+import ctypes as C
+import hashlib
+import json
+import os
+import struct
+
+import numpy as np
+import pytest
+
+import loader_files
+from minirender_gb300 import abi, capi, loaders
+from minirender_gb300 import workloads as W
+from oracle import oracle as O
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "loaders.json")
+MESH_KEYS = ("vertices", "normals", "texcoords", "indices", "normalsI", "texcoordsI")
+
+
+@pytest.fixture(scope="module")
+def files(tmp_path_factory):
+    d = str(tmp_path_factory.mktemp("models"))
+    return d, loader_files.write_all(d)
+
+
+def product_model(path):
+    """The product's model as the oracle flattens the reference's: nodes,
+    mesh arrays and textures decoded as loadPPM does (b / 255.0f)."""
+    L = capi.lib()
+    h = C.c_void_p()
+    rc = L.mr_model_load(path.encode(), C.byref(h))
+    if rc != 0:
+        return None
+    try:
+        nn, nm, nt = C.c_int32(), C.c_int32(), C.c_int32()
+        L.mr_model_counts(h, C.byref(nn), C.byref(nm), C.byref(nt))
+        nodes = (abi.mr_node * max(1, nn.value))()
+        assert L.mr_model_nodes(h, nodes, nn.value) == 0
+        meshes = []
+        for i in range(nm.value):
+            d = abi.mr_mesh_desc()
+            assert L.mr_model_mesh(h, i, C.byref(d)) == 0
+            def arr(p, n, dt, cols):
+                if n == 0:
+                    return np.zeros((0, cols) if cols else 0, dt)
+                ct = C.c_float if dt == np.float32 else C.c_int32
+                a = np.ctypeslib.as_array(C.cast(p, C.POINTER(ct)), shape=(n * (cols or 1),)).copy()
+                return a.reshape(-1, cols) if cols else a
+            meshes.append({"vertices": arr(d.vertices, d.n_vertices, np.float32, 3),
+                           "normals": arr(d.normals, d.n_normals, np.float32, 3),
+                           "texcoords": arr(d.texcoords, d.n_texcoords, np.float32, 2),
+                           "indices": arr(d.indices, d.n_indices, np.int32, 0),
+                           "normalsI": arr(d.normalsI, d.n_normalsI, np.int32, 0),
+                           "texcoordsI": arr(d.texcoordsI, d.n_texcoordsI, np.int32, 0)})
+        textures = []
+        for i in range(nt.value):
+            p, r, c = C.POINTER(C.c_uint8)(), C.c_int32(), C.c_int32()
+            assert L.mr_model_texture(h, i, C.byref(p), C.byref(r), C.byref(c)) == 0
+            b = np.ctypeslib.as_array(p, shape=(r.value * c.value * 3,)).copy().reshape(r.value, c.value, 3)
+            textures.append(b.astype(np.float32) / np.float32(255))
+        return {"nodes": nodes[:nn.value], "meshes": meshes, "textures": textures}
+    finally:
+        L.mr_model_free(h)
+
+
+def canonical(model):
+    """Byte serialisation of a flattened model (texture indices replaced by
+    the texture's pixels, so shared or duplicated textures compare equal)."""
+    if model is None:
+        return b"null"
+    out = [struct.pack("<i", len(model["nodes"]))]
+    for nd in model["nodes"]:
+        out.append(struct.pack("<iii", nd.parent, nd.mesh, nd.has_material))
+        out.append(np.array(nd.transform[:], np.float32).tobytes())
+        if nd.has_material:
+            m = nd.material
+            out.append(np.array(list(m.diffuse) + list(m.specular) + list(m.emissive) + [m.shininess],
+                                np.float32).tobytes())
+            t = model["textures"][m.texture] if m.texture >= 0 else None
+            out.append(b"notex" if t is None else struct.pack("<ii", *t.shape[:2]) + t.astype(np.float32).tobytes())
+    for m in model["meshes"]:
+        for k in MESH_KEYS:
+            out.append(k.encode() + struct.pack("<q", m[k].size) + np.ascontiguousarray(m[k]).tobytes())
+    return b"".join(out)
+
+
+def digest(model):
+    return hashlib.sha256(canonical(model)).hexdigest()
+
+
+def _golden():
+    with open(GOLDEN) as f:
+        return json.load(f)
+
+
+def test_models_match_golden(files, product_lib):
+    d, names = files
+    g = _golden()
+    for n in names:
+        assert digest(product_model(os.path.join(d, n))) == g[n], n
+
+
+def test_models_match_reference(files, product_lib, ref_lib):
+    d, names = files
+    for n in names:
+        p = os.path.join(d, n)
+        ref = O.ref_load_mesh(p)
+        got = product_model(p)
+        assert (ref is None) == (got is None), n
+        assert len(got["nodes"]) == len(ref["nodes"]), n
+        for a, b in zip(got["nodes"], ref["nodes"]):
+            assert (a.parent, a.mesh, a.has_material) == (b.parent, b.mesh, b.has_material), n
+        for i, (a, b) in enumerate(zip(got["meshes"], ref["meshes"])):
+            for k in MESH_KEYS:
+                assert np.array_equal(a[k].view(np.uint8), b[k].view(np.uint8)), (n, i, k)
+        assert canonical(got) == canonical(ref), n
+
+
+def test_python_scene_from_model(files, product_lib):
+    """load_mesh builds the scene-model objects the renderer mirror takes."""
+    d, names = files
+    node = loaders.load_mesh(os.path.join(d, "parts.obj"))
+    meshes = node.children
+    assert [type(m).__name__ for m in meshes] == ["TriMesh"] * 4  # "", nosuch, red, wood
+    wood = meshes[3]
+    assert wood.material.texture is not None and wood.material.texture.shape == (16, 24, 3)
+    assert np.isclose(float(meshes[2].material.shininess), 10.0)  # Ns 0 -> 10
+    assert all(m.indices.size % 3 == 0 for m in meshes)
+    x = loaders.load_mesh(os.path.join(d, "scene.x3d"))
+    assert len(x.children) >= 3
+
+
+def test_ppm_load_save_match_reference(tmp_path, product_lib, ref_lib):
+    rng = np.random.default_rng(5)
+    img = rng.integers(0, 256, (13, 29, 3)).astype(np.uint8)
+    p = str(tmp_path / "a.ppm")
+    loader_files._ppm(p, img, comment=True)
+    got = loaders.load_ppm(p)
+    assert np.array_equal(got, img)
+    assert np.array_equal((got.astype(np.float32) / np.float32(255)).view(np.uint32),
+                          O.ref_load_ppm(p).view(np.uint32))
+    # savePPM: the reference quantises floats; the library writes the bytes the device produced
+    f = rng.uniform(-0.2, 1.2, (7, 11, 3)).astype(np.float32)
+    q = O.quantize_rgb8(f)
+    a, b = str(tmp_path / "ref.ppm"), str(tmp_path / "gpu.ppm")
+    O.ref_save_ppm(a, f)
+    loaders.save_ppm(b, q)
+    assert open(a, "rb").read() == open(b, "rb").read()
+
+
+def test_stl_save_matches_reference(tmp_path, product_lib, ref_lib):
+    st, sc = W.config1(64, 48)
+    m = sc.children[0]
+    xf = np.array([[0.5, 0, 0.1, 1], [0, 2, 0, -1], [0.3, 0, 1, 0.25], [0, 0, 0, 1]], np.float32)
+    a, b = str(tmp_path / "ref.stl"), str(tmp_path / "gpu.stl")
+    O.ref_save_stl(a, m.desc(), xf)
+    loaders.save_stl(b, m, xf)
+    assert open(a, "rb").read() == open(b, "rb").read()
+
+
+def test_large_files_parsed_in_parallel_match_reference(tmp_path, product_lib, ref_lib):
+    """Binary STL above 200k facets and OBJ above 4 MB take the multi-threaded
+    paths; the result is the same as the reference's serial parse."""
+    rng = np.random.default_rng(8)
+    nf = 250_000
+    p = str(tmp_path / "big.stl")
+    rec = np.zeros(nf, dtype=[("f", "<f4", 12), ("a", "<i2")])
+    rec["f"] = rng.normal(size=(nf, 12)).astype(np.float32)
+    with open(p, "wb") as f:
+        f.write(b" " * 80 + struct.pack("<i", nf) + rec.tobytes())
+    assert canonical(product_model(p)) == canonical(O.ref_load_mesh(p))
+    q = str(tmp_path / "big.obj")
+    nv = 60_000
+    with open(q, "w") as f:
+        for v in rng.uniform(-1, 1, (nv, 3)).astype(np.float32):
+            f.write("v %r %r %r\n" % tuple(float(x) for x in v))
+        for v in rng.normal(size=(nv, 3)).astype(np.float32):
+            f.write("vn %r %r %r\n" % tuple(float(x) for x in v))
+        for k in range(60_000):
+            ids = rng.choice(nv, 3 + k % 2, replace=False) + 1
+            f.write("f " + " ".join(f"{i}//{i}" for i in ids) + "\n")
+    assert os.path.getsize(q) > 4 << 20
+    assert canonical(product_model(q)) == canonical(O.ref_load_mesh(q))
+
+
+def test_errors(tmp_path, product_lib):
+    L = capi.lib()
+    h = C.c_void_p()
+    assert L.mr_model_load(str(tmp_path / "missing.stl").encode(), C.byref(h)) == abi.MR_E_IO
+    bad = tmp_path / "bad.stl"
+    bad.write_bytes(b"nothing like an stl file here\n")
+    assert L.mr_model_load(str(bad).encode(), C.byref(h)) == abi.MR_E_IO
+    nx = tmp_path / "notx3d.x3d"
+    nx.write_text("<html><body/></html>")
+    assert L.mr_model_load(str(nx).encode(), C.byref(h)) == abi.MR_E_IO
+    other = tmp_path / "model.xyz"
+    other.write_text("1 2 3\n")
+    node = loaders.load_mesh(str(other))  # loadMesh: an empty node for other extensions
+    assert node.children == []
+    with pytest.raises(capi.MRError):
+        loaders.load_ppm(str(bad))

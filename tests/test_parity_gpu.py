@@ -113,3 +113,23 @@ def test_shared_and_separate_index_arrays(renderer):
         ctx.update_mesh(h, m.desc())
     finally:
         ctx.free_mesh(h)
+
+
+@pytest.mark.parametrize("name", ["textured.obj", "plain.obj", "scene.x3d", "binary.stl", "ascii.stl"])
+def test_loaded_models(renderer, tmp_path, name):
+    """Models read by the library's loaders (OBJ with material library and
+    texture, X3D with transforms and DEF/USE, binary and ASCII STL) render as
+    the oracle renders the same scene."""
+    import loader_files
+    from minirender_gb300 import loaders
+    from minirender_gb300 import projection as pj
+    from minirender_gb300.frame import FrameState
+    from minirender_gb300.scene import Scene
+    loader_files.write_all(str(tmp_path))
+    sc = Scene()
+    sc.add(loaders.load_mesh(str(tmp_path / name)))
+    st = FrameState(width=160, height=120,
+                    projection=pj.projection_frustum(pj.deg2rad(50), np.float32(160) / np.float32(120), 0.5, 100),
+                    view=pj.translate(0, 0, -6), light=np.array([0.3, 0.5, 1.0], np.float32),
+                    ambient=sc.ambientLight)
+    _check(f"loaded_{name}", st, sc, renderer)
