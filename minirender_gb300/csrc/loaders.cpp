@@ -72,7 +72,13 @@ bool read_file(const std::string& path, std::string& out) {
   FILE* f = fopen(path.c_str(), "rb");
   if (!f) return false;
   out.clear();
-  char buf[1 << 16];
+  long size = -1;
+  if (fseek(f, 0, SEEK_END) == 0) size = ftell(f);
+  if (size > 0 && fseek(f, 0, SEEK_SET) == 0) {  // one read into a buffer of the file's size
+    out.resize((size_t)size);
+    out.resize(fread(&out[0], 1, (size_t)size, f));
+  }
+  char buf[1 << 16];  // the rest (or all, for a stream without a size)
   size_t k;
   while ((k = fread(buf, 1, sizeof buf, f)) > 0) out.append(buf, k);
   fclose(f);
