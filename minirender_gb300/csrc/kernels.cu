@@ -18,11 +18,17 @@
 //                  barycentrics exactly, shades once per visible pixel and
 //                  writes RGB8/depth/ids            (src/Renderer.cpp:271-305, src/io.cpp:358-362)
 // Many frames per call (launch_batch):
-//   k_vertex, then k_setup_batch (every rasterised sub-triangle becomes a
-//   record, counted into its scene's tiles), then k_batch: one cooperative,
-//   persistent launch -- scan, scatter, and a dynamically scheduled loop over
-//   all tiles of all scenes that rasterises each tile into shared memory and
-//   resolves + shades its pixels in place (no frame-sized visibility buffer).
+//   k_vertex (when vertices are shared), a clear of the batch's visibility
+//   words (when small triangles are rasterised in the setup), then
+//   k_setup_batch (sub-triangles with a bounding box of at most small_max
+//   pixels rasterised into their scene's visibility words, larger ones
+//   become records counted into the scene's tiles), then k_batch: one
+//   cooperative, persistent launch -- scan, scatter, and a dynamically
+//   scheduled loop over all tiles of all scenes that rasterises each tile's
+//   records into shared memory (seeded with the small triangles' words),
+//   captures the winners' edge values and resolves + shades its pixels in
+//   place.  The PRE template flag is false for triangle soups: no vertex
+//   pass, kernels transform corners themselves.
 // Also: k_validate (index checks at upload), k_range (getRangeImage,
 // src/Renderer.cpp:388-415).
 //
@@ -1006,12 +1012,14 @@ __device__ __forceinline__ void raster_items(const BigRec* s_recs, const uint32_
 }
 
 // The batch's persistent kernel (cooperative launch, grid-wide barriers):
-//   1. exclusive scan of the per-tile counts (per-block segments + one block
-//      scanning the block sums), 2. scatter record indices into tile lists,
-//   3. tiles of all scenes taken from a work counter: each tile's records are
-//      staged in shared memory `chunk` at a time and rasterised into a
-//      shared-memory visibility tile, then every pixel of the tile is
-//      resolved, shaded and written to its scene's outputs.
+//   1. exclusive scan of the per-tile counts (per-block segments, then one
+//      block scanning the block sums), 2. scatter record indices into tile
+//      lists, 3. tiles of all scenes taken from a work counter: the tile's
+//      visibility words start from the scene's small-triangle words; its
+//      records are staged in shared memory `chunk` at a time and rasterised
+//      (pass 1), walked again to capture each winner's edge values (pass 2),
+//      then every pixel of the tile is resolved, shaded and written to its
+//      scene's outputs.
 // MINB: blocks of 256 threads per SM the register allocation must allow
 // (2: up to 128 registers per thread, for 64-thread blocks; 4: up to 64, so
 // that 128- and 256-thread blocks keep enough warps resident).
