@@ -215,7 +215,7 @@ typedef struct mr_batch_scene {
  * staged per pass in shared memory (16..256) for mr_render_batch. */
 MR_API int mr_set_batch_tuning(mr_ctx* ctx, int tile, int threads, int chunk);
 /* As mr_set_batch_tuning with a rectangular screen tile: power-of-two sides,
- * width 4..256, height 2..32, 64..1024 pixels.  Wide tiles shorten the
+ * width 4..256, height 2..64, 64..4096 pixels.  Wide tiles shorten the
  * column-by-column edge-function replay of triangles that cross tiles. */
 MR_API int mr_set_batch_tiling(mr_ctx* ctx, int tile_w, int tile_h, int threads, int chunk);
 /* Sub-triangles whose bounding box holds at most small_max pixels (0..4096,

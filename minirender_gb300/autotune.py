@@ -20,7 +20,7 @@ from . import capi
 
 # (tile width, tile height): square tiles plus wide ones, which shorten the
 # per-row edge replay of triangles crossing several tiles.
-SHAPES: List[Tuple[int, int]] = [(8, 8), (16, 16), (32, 16), (32, 32), (64, 16), (128, 8)]
+SHAPES: List[Tuple[int, int]] = [(8, 8), (16, 16), (32, 16), (32, 32), (64, 16), (128, 8), (64, 32), (64, 64)]
 CANDIDATES: List[Tuple[int, int, int, int]] = [(tw, th, t, ch) for tw, th in SHAPES for t in (64, 128, 256)
                                                for ch in (32, 64, 128)]
 

@@ -659,7 +659,7 @@ static cudaError_t pinned(T*& p, size_t& cap, size_t n) {
 MR_API int mr_set_batch_tiling(mr_ctx* c, int tile_w, int tile_h, int threads, int chunk) {
   if (!c) return MR_E_INVALID;
   if (!batch_tile_ok(tile_w, tile_h))
-    return fail(c, MR_E_INVALID, "tile sides must be powers of two, 4..256 x 2..32, 64..1024 pixels");
+    return fail(c, MR_E_INVALID, "tile sides must be powers of two, 4..256 x 2..64, 64..4096 pixels");
   if (threads != 64 && threads != 128 && threads != 256) return fail(c, MR_E_INVALID, "threads must be 64, 128 or 256");
   if (chunk < 16 || chunk > 256) return fail(c, MR_E_INVALID, "chunk must be in 16..256");
   std::lock_guard<std::recursive_mutex> g(c->mu);

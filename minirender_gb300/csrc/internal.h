@@ -21,10 +21,10 @@ cudaError_t launch_range(int W, int H, const float* dP, const float* depth, floa
 cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
                          cudaEvent_t* ev);
 int batch_grid(int tile_w, int tile_h, int chunk, int threads, bool pre);
-// Tile shapes k_batch takes: power-of-two sides, 64..1024 pixels (whole warps).
+// Tile shapes k_batch takes: power-of-two sides, 64..4096 pixels (whole warps).
 inline bool batch_tile_ok(int tw, int th) {
   auto pow2 = [](int v) { return v > 0 && (v & (v - 1)) == 0; };
-  return pow2(tw) && pow2(th) && tw >= 4 && tw <= 256 && th >= 2 && th <= 32 && tw * th >= 64 && tw * th <= 1024;
+  return pow2(tw) && pow2(th) && tw >= 4 && tw <= 256 && th >= 2 && th <= 64 && tw * th >= 64 && tw * th <= 4096;
 }
 }  // namespace mrg
 

@@ -80,7 +80,7 @@ def test_graph_replay_with_new_cameras(batch, refs):
 
 
 @pytest.mark.parametrize("tw,th,threads,chunk", [(64, 16, 128, 128), (128, 8, 64, 32), (256, 4, 256, 64),
-                                                  (4, 16, 64, 16)])
+                                                  (4, 16, 64, 16), (64, 64, 256, 128)])
 def test_batch_rectangular_tiles_same_result(batch, refs, tw, th, threads, chunk):
     batch.ctx.set_batch_graphs(True)
     batch.ctx.set_batch_tiling(tw, th, threads, chunk)
@@ -106,7 +106,8 @@ def test_batch_small_max_same_result(batch, refs, small_max):
 
 def test_batch_tiling_rejects_bad_shapes(batch):
     from minirender_gb300 import capi
-    for bad in [(48, 16, 64, 64), (512, 2, 64, 64), (8, 4, 64, 64), (64, 32, 64, 64), (16, 16, 96, 64)]:
+    for bad in [(48, 16, 64, 64), (512, 2, 64, 64), (8, 4, 64, 64), (64, 128, 64, 64), (128, 64, 64, 64),
+                (16, 16, 96, 64)]:
         with pytest.raises(capi.MRError):
             batch.ctx.set_batch_tiling(*bad)
     for bad in (-1, 4097):
