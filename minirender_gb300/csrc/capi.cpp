@@ -50,7 +50,6 @@ MR_API int mr_create(int device, mr_ctx** out) {
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_cnt, sizeof(Counters));
   for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming);
-  if (e == cudaSuccess) e = c->dP.ensure(16);
 
   if (e != cudaSuccess) {
     delete c;
@@ -73,10 +72,9 @@ MR_API int mr_destroy(mr_ctx* c) {
       if (t.mem) cudaFree(t.mem);
     c->vis.release(); c->rgb8.release(); c->depth.release(); c->rgbf.release();
     c->normals.release(); c->range.release(); c->ids.release(); c->recs.release();
-    c->bins.release(); c->tiles.release(); c->rs.release(); c->tri_base.release(); c->dP.release();
+    c->bins.release(); c->tiles.release(); c->stage.release();
     c->va.release(); c->vb.release(); c->vn.release();
-    if (c->h_rs) cudaFreeHost(c->h_rs);
-    if (c->h_tri_base) cudaFreeHost(c->h_tri_base);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->d_cnt) cudaFree(c->d_cnt);
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
     for (auto& e : c->ev)
@@ -348,9 +346,7 @@ MR_API int mr_texture_free(mr_ctx* c, int32_t h) {
 static int launch_last(mr_ctx* c) {
   FrameParams& F = c->last;
   cudaStream_t st = c->stream;
-  int ntiles = F.tiles_x * F.tiles_y;
-  CK(cudaMemsetAsync(c->d_cnt, 0, sizeof(Counters), st), "counter reset");
-  CK(cudaMemsetAsync(c->tiles.p, 0, sizeof(uint32_t) * (size_t)(3 * ntiles + 1), st), "tile reset");
+  // (the clear kernel also zeroes the counters and the tile tables)
   CK(launch_frame(F, st, c->profiling ? c->ev : nullptr), "frame launch");
   return MR_OK;
 }
@@ -378,13 +374,20 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   size_t nrs = (size_t)std::max(n, 1);
   if (c->h_rs_cap < nrs) {
     CK(cudaEventSynchronize(c->staged), "staging wait");
-    if (c->h_rs) cudaFreeHost(c->h_rs);
-    if (c->h_tri_base) cudaFreeHost(c->h_tri_base);
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    c->h_stage = nullptr;
     c->h_rs = nullptr;
     c->h_tri_base = nullptr;
+    c->h_P = nullptr;
     c->h_rs_cap = 0;
-    CK(cudaMallocHost(&c->h_rs, sizeof(DevRenderable) * nrs), "pinned staging");
-    CK(cudaMallocHost(&c->h_tri_base, sizeof(uint32_t) * 3 * (nrs + 1)), "pinned staging");
+    c->off_bases = align256(sizeof(DevRenderable) * nrs);
+    c->off_P = c->off_bases + align256(sizeof(uint32_t) * 3 * (nrs + 1));
+    c->stage_bytes = c->off_P + sizeof(float) * 16;
+    CK(cudaMallocHost(&c->h_stage, c->stage_bytes), "pinned staging");
+    CK(c->stage.ensure(c->stage_bytes), "staging buffer");
+    c->h_rs = (DevRenderable*)c->h_stage;
+    c->h_tri_base = (uint32_t*)(c->h_stage + c->off_bases);
+    c->h_P = (float*)(c->h_stage + c->off_P);
     c->h_rs_cap = nrs;
   } else {
     CK(cudaEventSynchronize(c->staged), "staging wait");
@@ -449,8 +452,6 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   CK(c->recs.ensure((size_t)2 * total), "record buffer");
   CK(c->tiles.ensure((size_t)3 * tx * ty + 1), "tile buffer");
   if (c->bins.cap < ((size_t)1 << 20)) CK(c->bins.ensure((size_t)1 << 20), "bin buffer");
-  CK(c->rs.ensure(nrs), "renderable table");
-  CK(c->tri_base.ensure(3 * (nrs + 1)), "base tables");
   // The per-vertex pass pays off when vertices are shared (each one used by
   // two or more triangle corners on average); for triangle soups every
   // corner is its own vertex and the kernels transform corners themselves.
@@ -460,9 +461,8 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     CK(c->vb.ensure(vbase), "vertex buffer");
     CK(c->vn.ensure(nbase), "normal buffer");
   }
-  CK(cudaMemcpyAsync(c->rs.p, c->h_rs, sizeof(DevRenderable) * n, cudaMemcpyHostToDevice, c->stream), "renderable upload");
-  CK(cudaMemcpyAsync(c->tri_base.p, c->h_tri_base, sizeof(uint32_t) * 3 * (n + 1), cudaMemcpyHostToDevice, c->stream), "base upload");
-  CK(cudaMemcpyAsync(c->dP.p, f->projection, sizeof(float) * 16, cudaMemcpyHostToDevice, c->stream), "projection upload");
+  memcpy(c->h_P, f->projection, sizeof(float) * 16);
+  CK(cudaMemcpyAsync(c->stage.p, c->h_stage, c->stage_bytes, cudaMemcpyHostToDevice, c->stream), "staging upload");
   CK(cudaEventRecord(c->staged, c->stream), "staging event");
 
   FrameParams& F = c->last;
@@ -489,10 +489,11 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   F.tiles_x = tx;
   F.tiles_y = ty;
   F.small_max = c->small_max;
-  F.g.rs = c->rs.p;
-  F.g.tri_base = c->tri_base.p;
-  F.g.vert_base = c->tri_base.p + (n + 1);
-  F.g.nrm_base = c->tri_base.p + 2 * (n + 1);
+  const uint32_t* d_bases = (const uint32_t*)(c->stage.p + c->off_bases);
+  F.g.rs = (const DevRenderable*)c->stage.p;
+  F.g.tri_base = d_bases;
+  F.g.vert_base = d_bases + (n + 1);
+  F.g.nrm_base = d_bases + 2 * (n + 1);
   F.g.n_verts = (uint32_t)vbase;
   F.g.n_nrms = (uint32_t)nbase;
   F.g.va = vertex_pass ? c->va.p : nullptr;  // null: kernels transform per corner
@@ -616,7 +617,8 @@ MR_API int mr_read_range_image(mr_ctx* c, float* xyz) {
   if (!c->last.depth) return fail(c, MR_E_INVALID, "depth was not requested for this frame");
   size_t npx = (size_t)c->last.v.W * c->last.v.H;
   CK(c->range.ensure(3 * npx), "range buffer");
-  CK(launch_range(c->last.v.W, c->last.v.H, c->dP.p, c->last.depth, c->range.p, c->stream), "range launch");
+  CK(launch_range(c->last.v.W, c->last.v.H, (const float*)(c->stage.p + c->off_P), c->last.depth, c->range.p,
+                  c->stream), "range launch");
   CK(cudaMemcpyAsync(xyz, c->range.p, 12 * npx, cudaMemcpyDeviceToHost, c->stream), "range read");
   CK(cudaStreamSynchronize(c->stream), "range wait");
   return rc;

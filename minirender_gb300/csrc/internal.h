@@ -134,14 +134,16 @@ struct mr_ctx {
   DevBuf<BigRec> recs;
   DevBuf<uint32_t> bins;
   DevBuf<uint32_t> tiles;
-  DevBuf<DevRenderable> rs;
-  DevBuf<uint32_t> tri_base;   // tri, vertex and normal base tables, 3 x (n+1)
+  // Per-frame staging, one block on both sides (one copy per frame):
+  // renderables (cap) | tri, vertex and normal base tables 3 x (cap+1) | projection
+  DevBuf<unsigned char> stage;
+  unsigned char* h_stage = nullptr;
+  size_t h_rs_cap = 0, stage_bytes = 0, off_bases = 0, off_P = 0;
+  DevRenderable* h_rs = nullptr;
+  uint32_t* h_tri_base = nullptr;
+  float* h_P = nullptr;
   DevBuf<float4> va, vn;        // per-frame vertex-pass outputs
   DevBuf<float2> vb;
-  DevBuf<float> dP;
-  DevRenderable* h_rs = nullptr;
-  size_t h_rs_cap = 0;
-  uint32_t* h_tri_base = nullptr;
   Counters* d_cnt = nullptr;
   Counters* h_cnt = nullptr;
   cudaEvent_t ev[8] = {};

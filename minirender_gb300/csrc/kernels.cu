@@ -480,9 +480,13 @@ __device__ __forceinline__ void resolve_pixel(const View& V, const Geo& G, int r
 __device__ __forceinline__ uint8_t to_byte(float v) { return (uint8_t)(int)clampr(v * 255.0f, 0.0f, 255.0f); }
 
 // ------------------------------------------------------------------ kernels
-__global__ void k_clear(unsigned long long* vis, size_t n) {
+// vis[0..n) = VIS_EMPTY; also zeroes z[0..nz) (a frame's counters and tile
+// tables, so they need no separate memset before the frame).
+__global__ void k_clear(unsigned long long* vis, size_t n, uint32_t* z0, uint32_t nz0, uint32_t* z1, uint32_t nz1) {
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t k = i; k < nz0; k += stride) z0[k] = 0;
+  for (size_t k = i; k < nz1; k += stride) z1[k] = 0;
   for (; i < n; i += stride) vis[i] = VIS_EMPTY;
 }
 
@@ -1281,7 +1285,9 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   // The clear also brings vis[] into L2 (write-allocate), so the setup
   // kernel's atomics hit L2.
   int cgrid = grid_for(npx, 256);
-  k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(F.vis, npx);
+  k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(
+      F.vis, npx, reinterpret_cast<uint32_t*>(F.counters), (uint32_t)(sizeof(Counters) / 4), F.tile_count,
+      (uint32_t)(3 * F.tiles_x * F.tiles_y + 1));
   if (pre && (F.g.n_verts + F.g.n_nrms) > 0)
     k_vertex<<<grid_for((size_t)F.g.n_verts + F.g.n_nrms, 256), 256, 0, st>>>(F.g, F.v, nullptr);
   if (ev) cudaEventRecord(ev[1], st);
@@ -1340,7 +1346,7 @@ cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* 
   }
   if (B.small_max > 0 && B.n_px) {  // small triangles' visibility words of every scene
     int cgrid = grid_for(B.n_px, 256);
-    k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(B.vis, B.n_px);
+    k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(B.vis, B.n_px, nullptr, 0, nullptr, 0);
   }
   if (ev) cudaEventRecord(ev[1], st);
   if (B.g.n_tris) {
