@@ -42,6 +42,8 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "raster.cuh"
 
 namespace cg = cooperative_groups;
@@ -49,6 +51,14 @@ namespace cg = cooperative_groups;
 namespace mrg {
 
 // ------------------------------------------------------------------ helpers
+// Programmatic dependent launch (sm_90+): a kernel launched with programmatic
+// stream serialisation may be scheduled while its predecessor is finishing;
+// pdl_wait() blocks until the predecessor grid has completed and its writes
+// are visible (a no-op for a kernel launched the ordinary way); pdl_trigger()
+// lets the successor's blocks start launching.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+
 __device__ __forceinline__ int find_base(const uint32_t* base, int lo, int hi, uint32_t g) {
   while (hi - lo > 1) {
     int mid = (lo + hi) >> 1;
@@ -483,6 +493,7 @@ __device__ __forceinline__ uint8_t to_byte(float v) { return (uint8_t)(int)clamp
 // vis[0..n) = VIS_EMPTY; also zeroes z[0..nz) (a frame's counters and tile
 // tables, so they need no separate memset before the frame).
 __global__ void k_clear(unsigned long long* vis, size_t n, uint32_t* z0, uint32_t nz0, uint32_t* z1, uint32_t nz1) {
+  pdl_trigger();
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t k = i; k < nz0; k += stride) z0[k] = 0;
@@ -511,6 +522,8 @@ __global__ void k_validate(DevMesh M, uint32_t* bad) {
 // threads [n_verts, n_verts + n_nrms) transform normals.  The view of a
 // vertex is scenes[R.scene].v for batches, V otherwise.
 __global__ void __launch_bounds__(256) k_vertex(Geo G, View V, const SceneRec* scenes) {
+  pdl_wait();
+  pdl_trigger();
   uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   if (g < G.n_verts) {
     const DevRenderable& R = G.rs[find_base(G.vert_base, 0, G.n_renderables, g)];
@@ -639,6 +652,7 @@ __device__ __forceinline__ void raster_small(const Setup (&S)[2], const int (&ki
 
 template <bool PRE>
 __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
+  pdl_wait();
   __shared__ SmallRec s_rec[kSetupWarps][64];
   __shared__ int s_pre[kSetupWarps][65];
   __shared__ BlockCounters bc;
@@ -720,6 +734,7 @@ constexpr int kBinThreads = 256;
 // merged into vis[].  With no large record every block returns at once,
 // before any barrier.
 __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
+  pdl_trigger();
   extern __shared__ unsigned long long svis[];
   __shared__ uint32_t part[kBinThreads];
   const uint32_t nrec = min(F.counters->rec_count, F.rec_cap);
@@ -796,6 +811,7 @@ __global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
 constexpr int kResolveTileW = 32, kResolveTileH = 8;
 template <bool PRE>
 __global__ void __launch_bounds__(256, 4) k_resolve(FrameParams F) {
+  pdl_wait();
   // loadPPM's texel decode b/255.0f (src/io.cpp:410), one division per byte value
   __shared__ float s_dec[256];
   s_dec[threadIdx.x] = (float)threadIdx.x / 255.0f;
@@ -1261,6 +1277,23 @@ cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// Ordinary launch allowed to overlap its predecessor's tail (the kernel calls
+// pdl_wait() before touching anything the predecessor writes).
+template <typename... Exp, typename... Act>
+static cudaError_t launch_after(void (*k)(Exp...), int grid, int block, cudaStream_t st, Act&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(block);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, std::forward<Act>(args)...);
+}
+
 static cudaError_t launch_coop(const void* fn, int grid, int block, void** args, size_t smem, cudaStream_t st) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(grid);
@@ -1288,12 +1321,17 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(
       F.vis, npx, reinterpret_cast<uint32_t*>(F.counters), (uint32_t)(sizeof(Counters) / 4), F.tile_count,
       (uint32_t)(3 * F.tiles_x * F.tiles_y + 1));
+  // vertex pass, setup and resolve may be scheduled while their predecessor
+  // finishes (they wait for it before reading its output)
+  cudaError_t le = cudaSuccess;
   if (pre && (F.g.n_verts + F.g.n_nrms) > 0)
-    k_vertex<<<grid_for((size_t)F.g.n_verts + F.g.n_nrms, 256), 256, 0, st>>>(F.g, F.v, nullptr);
+    le = launch_after(k_vertex, grid_for((size_t)F.g.n_verts + F.g.n_nrms, 256), 256, st, F.g, F.v,
+                      (const SceneRec*)nullptr);
+  if (le != cudaSuccess) return le;
   if (ev) cudaEventRecord(ev[1], st);
   if (F.g.n_tris) {
-    if (pre) k_setup<true><<<grid_for(F.g.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(F);
-    else k_setup<false><<<grid_for(F.g.n_tris, kSetupThreads), kSetupThreads, 0, st>>>(F);
+    le = launch_after(pre ? k_setup<true> : k_setup<false>, grid_for(F.g.n_tris, kSetupThreads), kSetupThreads, st, F);
+    if (le != cudaSuccess) return le;
   }
   if (ev) cudaEventRecord(ev[2], st);
   {
@@ -1311,8 +1349,8 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   if (ev) cudaEventRecord(ev[3], st);
   if (ev) cudaEventRecord(ev[4], st);
   const int rgrid = ((F.v.W + kResolveTileW - 1) / kResolveTileW) * ((F.v.H + kResolveTileH - 1) / kResolveTileH);
-  if (pre) k_resolve<true><<<rgrid, 256, 0, st>>>(F);
-  else k_resolve<false><<<rgrid, 256, 0, st>>>(F);
+  le = launch_after(pre ? k_resolve<true> : k_resolve<false>, rgrid, 256, st, F);
+  if (le != cudaSuccess) return le;
   if (ev) cudaEventRecord(ev[5], st);
   return cudaGetLastError();
 }
