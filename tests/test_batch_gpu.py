@@ -138,3 +138,19 @@ def test_batch_of_triangle_soups(batch):
             _check_all(batch, items, refs, f"soup{small_max}")
     finally:
         batch.ctx.set_batch_small_max(64)
+
+
+def test_batch_with_empty_scenes(batch):
+    """Scenes without renderables or with empty meshes come out as background
+    (and do not disturb the other scenes of the batch)."""
+    from minirender_gb300.scene import Scene, TriMesh
+    st1, sc1 = W.config1(96, 64)
+    empty = Scene()
+    st_e = W.config1(80, 48)[0]
+    hollow = Scene()
+    hollow.add(TriMesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros(0, np.int32)))
+    items = [(st_e, empty), (st1, sc1), (st_e, hollow)]
+    refs = [O.render(st, sc) for st, sc in items]
+    batch.ctx.set_batch_graphs(False)
+    _check_all(batch, items, refs, "empty")
+    batch.ctx.set_batch_graphs(True)

@@ -133,3 +133,14 @@ def test_loaded_models(renderer, tmp_path, name):
                     view=pj.translate(0, 0, -6), light=np.array([0.3, 0.5, 1.0], np.float32),
                     ambient=sc.ambientLight)
     _check(f"loaded_{name}", st, sc, renderer)
+
+
+def test_empty_frames(renderer):
+    """A frame without renderables, and one whose only mesh is empty, render the
+    background (depth 1e11, no triangle ids) as the reference does."""
+    from minirender_gb300.scene import Scene, TriMesh
+    st, _ = W.config1(64, 48)
+    _check("empty_scene", st, Scene(), renderer)
+    sc = Scene()
+    sc.add(TriMesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros(0, np.int32)))
+    _check("empty_mesh", st, sc, renderer)

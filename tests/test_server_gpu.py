@@ -144,3 +144,20 @@ def test_server_other_tunings_same_result(ctx):
                 assert _same(out, refs[i]), f"request {i} differs with {opts}"
         finally:
             srv.close()
+
+
+def test_server_empty_mesh_request(ctx):
+    """A request whose mesh has no triangles completes with the background."""
+    from minirender_gb300.server import RenderServer
+    from minirender_gb300.scene import TriMesh
+    st, _ = W.config1(64, 48)
+    m = TriMesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros(0, np.int32))
+    srv = RenderServer(ctx, budget_bytes=1 << 30, slots=1, max_batch=4)
+    try:
+        out = _buffers(st)
+        t = srv.submit(st, m, mesh_key=42, out=out)
+        assert srv.wait(t).status == 0
+        ref = _oracle(st, m)
+        assert _same(out, ref)
+    finally:
+        srv.close()
