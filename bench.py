@@ -53,6 +53,8 @@ def parse():
     p.add_argument("--requests", type=int, default=1500, help="requests per rate (config5)")
     p.add_argument("--serve-tuning", default="16,16,64,64,64",
                    help="tile_w,tile_h,threads,chunk,small_max of the render server's batches (config5)")
+    p.add_argument("--serve-slots", type=int, default=3, help="render server batch slots (config5)")
+    p.add_argument("--serve-max-batch", type=int, default=64, help="render server requests per batch (config5)")
     p.add_argument("--scenes", type=int, default=256, help="scenes per batch (config4)")
     p.add_argument("--tuning", default="",
                    help="tile,threads,chunk or tile_w,tile_h,threads,chunk[,small_max] for batches "
@@ -463,8 +465,8 @@ def serve_arm(args, ws, rank, local):
         _pin_mesh(m)
     ctx = capi.Context(local)
     tw, th, tthreads, tchunk, tsmall = (int(x) for x in args.serve_tuning.split(","))
-    srv = RenderServer(ctx, budget_bytes=40 << 30, slots=3, max_batch=64, tile=tw, tile_h=th, threads=tthreads,
-                       chunk=tchunk, small_max=tsmall)
+    srv = RenderServer(ctx, budget_bytes=40 << 30, slots=args.serve_slots, max_batch=args.serve_max_batch, tile=tw,
+                       tile_h=th, threads=tthreads, chunk=tchunk, small_max=tsmall)
     maxpx = 3840 * 2160
     ring = [torch.empty(maxpx * 3, dtype=torch.uint8).pin_memory().numpy() for _ in range(96)]
     ring_ticket = [None] * len(ring)
@@ -527,7 +529,7 @@ def serve_arm(args, ws, rank, local):
         "config": {"workload": "Poisson request stream; each request a triangle soup with log-uniform "
                                "1k-2M triangles at log-uniform 128x128..3840x2160, 30% re-render a "
                                "resident mesh with a new camera; 40 GB device budget; RGB8 read back",
-                   "server": {"slots": 3, "max_batch": 64,
+                   "server": {"slots": args.serve_slots, "max_batch": args.serve_max_batch,
                               "tuning": {"tile_w": tw, "tile_h": th, "threads": tthreads, "chunk": tchunk,
                                          "small_max": tsmall}}},
         "rates": served, "capacity": cap,

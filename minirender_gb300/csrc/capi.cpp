@@ -179,7 +179,8 @@ static size_t mesh_bytes(const mr_mesh_desc* d, bool has_uv) {
          align256((size_t)4 * ((ntri + 31) / 32 + 1));
 }
 
-int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes) {
+int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes,
+                cudaMemPool_t pool) {
   int rc = check_desc(c, d);
   if (rc) return rc;
   MeshRec m;
@@ -193,7 +194,9 @@ int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* 
   m.bytes = mesh_bytes(d, m.d.has_uv);
   m.stream_ordered = stream != nullptr;
   cudaStream_t st = stream ? stream : c->stream;
-  if (stream) CK(cudaMallocAsync(&m.mem, m.bytes, stream), "mesh allocation");
+  if (stream)
+    CK(pool ? cudaMallocFromPoolAsync(&m.mem, m.bytes, pool, stream) : cudaMallocAsync(&m.mem, m.bytes, stream),
+       "mesh allocation");
   else CK(cudaMalloc(&m.mem, m.bytes), "mesh allocation");
   rc = copy_mesh(c, m, d, st);
   if (rc) {
@@ -262,7 +265,7 @@ MR_API int mr_mesh_free(mr_ctx* c, int32_t h) {
 }
 
 int texture_create(mr_ctx* c, const void* data, bool rgb8, int32_t rows, int32_t cols, cudaStream_t stream,
-                   int32_t* out) {
+                   int32_t* out, cudaMemPool_t pool) {
   if (!out || !data || rows <= 0 || cols <= 0) return fail(c, MR_E_INVALID, "bad texture");
   TexRec t;
   t.live = true;
@@ -272,7 +275,9 @@ int texture_create(mr_ctx* c, const void* data, bool rgb8, int32_t rows, int32_t
   t.bytes = (size_t)rows * cols * (rgb8 ? 3 : 12);
   t.stream_ordered = stream != nullptr;
   cudaStream_t st = stream ? stream : c->stream;
-  if (stream) CK(cudaMallocAsync(&t.mem, t.bytes, stream), "texture allocation");
+  if (stream)
+    CK(pool ? cudaMallocFromPoolAsync(&t.mem, t.bytes, pool, stream) : cudaMallocAsync(&t.mem, t.bytes, stream),
+       "texture allocation");
   else CK(cudaMalloc(&t.mem, t.bytes), "texture allocation");
   cudaError_t e = cudaMemcpyAsync(t.mem, data, t.bytes, cudaMemcpyHostToDevice, st);
   if (e != cudaSuccess) {

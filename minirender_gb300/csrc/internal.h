@@ -187,9 +187,11 @@ int batch_run(mr_ctx* c, BatchSlot& B, cudaStream_t st, bool profiling, cudaEven
 int batch_settle(mr_ctx* c, BatchSlot& B, cudaStream_t st);
 // Resident meshes/textures; with `stream` the memory is stream-ordered
 // (cudaMallocAsync / cudaFreeAsync) so no device-wide synchronisation occurs.
-int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes);
+// stream != null: stream-ordered allocation (from `pool` when given).
+int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes,
+                cudaMemPool_t pool = nullptr);
 int mesh_destroy(mr_ctx* c, int32_t h, cudaStream_t stream);
 int texture_create(mr_ctx* c, const void* data, bool rgb8, int32_t rows, int32_t cols, cudaStream_t stream,
-                   int32_t* out);
+                   int32_t* out, cudaMemPool_t pool = nullptr);
 int texture_destroy(mr_ctx* c, int32_t h, cudaStream_t stream);
 }  // extern "C"

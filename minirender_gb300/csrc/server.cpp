@@ -88,6 +88,10 @@ struct mr_server {
   size_t committed = 0, resident = 0;
   uint64_t use_clock = 0;
   std::vector<Slot*> slots;
+  // Meshes and textures come from a pool of the server's own that keeps up
+  // to the budget mapped between uses (the default pool would return freed
+  // memory to the system at every synchronisation and map it again).
+  cudaMemPool_t pool = nullptr;
   std::thread worker;
   bool stop = false;
   uint64_t next_ticket = 1;
@@ -269,7 +273,7 @@ void mr_server::run() {
         if (!meshes.count(r->mesh_key)) {
           Cached e;
           std::lock_guard<std::recursive_mutex> g(c->mu);
-          rc = mesh_create(c, &r->req.mesh, s->stream, &e.handle, &e.bytes);
+          rc = mesh_create(c, &r->req.mesh, s->stream, &e.handle, &e.bytes, pool);
           if (rc == MR_OK && (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
                               cudaEventRecord(e.ready, s->stream) != cudaSuccess))
             rc = MR_E_CUDA;
@@ -284,7 +288,7 @@ void mr_server::run() {
           e.bytes = (size_t)r->req.tex_rows * r->req.tex_cols * 3;
           std::lock_guard<std::recursive_mutex> g(c->mu);
           rc = texture_create(c, r->req.texture_rgb8, true, r->req.tex_rows, r->req.tex_cols, s->stream,
-                              &e.handle);
+                              &e.handle, pool);
           if (rc == MR_OK && (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
                               cudaEventRecord(e.ready, s->stream) != cudaSuccess))
             rc = MR_E_CUDA;
@@ -335,6 +339,19 @@ MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out)
   s->c = c;
   s->o = *o;
   cudaSetDevice(c->device);
+  {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = c->device;
+    uint64_t keep = o->budget_bytes;
+    if (cudaMemPoolCreate(&s->pool, &props) != cudaSuccess ||
+        cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep) != cudaSuccess) {
+      if (s->pool) cudaMemPoolDestroy(s->pool);
+      delete s;
+      return MR_E_CUDA;
+    }
+  }
   for (int i = 0; i < o->slots; i++) {
     Slot* sl = new Slot();
     sl->b.tile_w = tw;
@@ -349,6 +366,7 @@ MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out)
         cudaStreamDestroy(x->stream);
         delete x;
       }
+      cudaMemPoolDestroy(s->pool);
       delete s;
       return MR_E_CUDA;
     }
@@ -467,6 +485,7 @@ MR_API int mr_server_destroy(mr_server* s) {
       cudaStreamDestroy(sl->stream);
       delete sl;
     }
+    if (s->pool) cudaMemPoolDestroy(s->pool);  // every allocation from it has been freed
   }
   for (auto& kv : s->reqs) delete kv.second;
   delete s;
