@@ -54,7 +54,7 @@ def parse():
     p.add_argument("--serve-tuning", default="16,16,64,64,64",
                    help="tile_w,tile_h,threads,chunk,small_max of the render server's batches (config5)")
     p.add_argument("--serve-slots", type=int, default=3, help="render server batch slots (config5)")
-    p.add_argument("--serve-max-batch", type=int, default=64, help="render server requests per batch (config5)")
+    p.add_argument("--serve-max-batch", type=int, default=16, help="render server requests per batch (config5)")
     p.add_argument("--scenes", type=int, default=256, help="scenes per batch (config4)")
     p.add_argument("--tuning", default="",
                    help="tile,threads,chunk or tile_w,tile_h,threads,chunk[,small_max] for batches "
