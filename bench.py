@@ -236,13 +236,12 @@ def cpu_frames_per_s(st, sc, n_threads: int, frames: int):
     return frames / secs, secs
 
 
-STAGES = ["clear+vertex", "setup", "bin", "tile_raster", "resolve"]
+STAGES = ["clear+vertex", "setup", "large_raster", "-", "resolve"]
 TUNING_KEYS = ("tile_w", "tile_h", "threads", "chunk", "small_max")
-# kernels between the stage events of one plain frame (the binning and tile
-# raster of large triangles are one cooperative kernel; "tile_raster" is the
-# empty interval after it)
-KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "bin": "k_bin_tile",
-           "tile_raster": "k_bin_tile", "resolve": "k_resolve"}
+# kernels between the stage events of one plain frame ("-" is an empty
+# interval kept so the stage list keeps its five slots)
+KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "large_raster": "k_raster_large",
+           "-": "k_raster_large", "resolve": "k_resolve"}
 
 
 def e2e_legs(args, ws, r, sc, st, flat, frame, rs, n, mesh_bytes, tex_bytes):
@@ -683,8 +682,10 @@ def gpu_arm(args, ws, rank, local):
     alg = {
         "clear+vertex": 8 * P + (12 * V + 24 * V + 16 * V if vertex_pass else 0),
         "setup": 12 * T + 12 * V + 64 * n_big,
-        "bin": 2 * 64 * n_big + 8 * int(stats.bin_entries),
-        "tile_raster": 64 * int(stats.bin_entries),
+        # row blocks (8 B each) and their records; the vis words it updates
+        # are the clear's, resident in L2
+        "large_raster": 8 * int(stats.bin_entries) + 64 * n_big,
+        "-": 0,
         "resolve": 8 * P + 7 * P + 3 * tex_px,
     }
     peak, peak_kind = peaks()
@@ -718,7 +719,7 @@ def gpu_arm(args, ws, rank, local):
         "counters": {"clipped": int(stats.clipped), "rasterised": int(stats.rasterised),
                      "small_direct": int(stats.small_direct), "binned": int(stats.binned),
                      "bin_entries": int(stats.bin_entries)},
-        # k_clear, [k_vertex], k_setup, k_bin_tile, k_resolve per frame
+        # k_clear, [k_vertex], k_setup, k_raster_large, k_resolve per frame
         "gpu_launches": (5 if vertex_pass else 4) * args.steps,
         "clocks": clk,
     }

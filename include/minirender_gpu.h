@@ -142,10 +142,11 @@ typedef struct mr_stats {
     int64_t clipped;          /* triangles that crossed the near plane */
     int64_t rasterised;       /* sub-triangles past cull and reject */
     int64_t small_direct;     /* rasterised in the setup kernel */
-    int64_t binned;           /* sub-triangles sent to tile bins */
-    int64_t bin_entries;      /* (tile, sub-triangle) pairs */
+    int64_t binned;           /* large sub-triangles (records) */
+    int64_t bin_entries;      /* their work items: 32-row blocks (mr_render),
+                                 (tile, sub-triangle) pairs (mr_render_batch) */
     int64_t error_flags;      /* nonzero: MR_E_BAD_INDEX seen */
-    float stage_ms[8];        /* when profiling: clear, setup, bin, raster, resolve, ... */
+    float stage_ms[8];        /* when profiling: clear+vertex, setup, large raster, -, resolve */
     int32_t n_stages;
 } mr_stats;
 
@@ -160,7 +161,9 @@ MR_API int mr_destroy(mr_ctx* ctx);
 /* cudaStream_t passed as void*; NULL = the context's own stream. */
 MR_API int mr_set_stream(mr_ctx* ctx, void* cuda_stream);
 MR_API int mr_synchronize(mr_ctx* ctx);
-/* Tile edge (pixels, 8/16/32) and small-triangle bounding-box limit. */
+/* Small-triangle bounding-box limit (pixels) of mr_render.  `tile` (8, 16
+ * or 32) is validated and kept for source compatibility; single frames no
+ * longer bin into tiles. */
 MR_API int mr_set_tuning(mr_ctx* ctx, int tile, int small_max);
 MR_API int mr_set_profiling(mr_ctx* ctx, int on);
 

@@ -72,7 +72,7 @@ MR_API int mr_destroy(mr_ctx* c) {
       if (t.mem) cudaFree(t.mem);
     c->vis.release(); c->rgb8.release(); c->depth.release(); c->rgbf.release();
     c->normals.release(); c->range.release(); c->ids.release(); c->recs.release();
-    c->bins.release(); c->tiles.release(); c->stage.release();
+    c->items.release(); c->stage.release();
     c->va.release(); c->vb.release(); c->vn.release();
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->d_cnt) cudaFree(c->d_cnt);
@@ -446,8 +446,6 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
 
   const int W = f->width, H = f->height;
   const size_t npx = (size_t)W * H;
-  const int TS = c->tile;
-  const int tx = (W + TS - 1) / TS, ty = (H + TS - 1) / TS;
   CK(c->vis.ensure(npx), "vis buffer");
   if (outputs & MR_OUT_RGB8) CK(c->rgb8.ensure(3 * npx), "rgb8 buffer");
   if (outputs & MR_OUT_DEPTH) CK(c->depth.ensure(npx), "depth buffer");
@@ -455,8 +453,7 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   if (outputs & MR_OUT_TRI_ID) CK(c->ids.ensure(npx), "id buffer");
   if (f->save_normals) CK(c->normals.ensure(3 * npx), "normals buffer");
   CK(c->recs.ensure((size_t)2 * total), "record buffer");
-  CK(c->tiles.ensure((size_t)3 * tx * ty + 1), "tile buffer");
-  if (c->bins.cap < ((size_t)1 << 20)) CK(c->bins.ensure((size_t)1 << 20), "bin buffer");
+  if (c->items.cap < ((size_t)1 << 18)) CK(c->items.ensure((size_t)1 << 18), "row-block buffer");
   // The per-vertex pass pays off when vertices are shared (each one used by
   // two or more triangle corners on average); for triangle soups every
   // corner is its own vertex and the kernels transform corners themselves.
@@ -490,9 +487,6 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   memcpy(F.v.bg, f->background, sizeof(F.v.bg));
   F.g.n_renderables = n;
   F.g.n_tris = (uint32_t)total;
-  F.tile = TS;
-  F.tiles_x = tx;
-  F.tiles_y = ty;
   F.small_max = c->small_max;
   const uint32_t* d_bases = (const uint32_t*)(c->stage.p + c->off_bases);
   F.g.rs = (const DevRenderable*)c->stage.p;
@@ -507,11 +501,8 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   F.vis = c->vis.p;
   F.recs = c->recs.p;
   F.rec_cap = (uint32_t)std::min<size_t>(c->recs.cap, 0xFFFFFFFFu);
-  F.tile_count = c->tiles.p;
-  F.tile_fill = c->tiles.p + (size_t)tx * ty;
-  F.tile_start = c->tiles.p + (size_t)2 * tx * ty;
-  F.bins = c->bins.p;
-  F.bin_cap = (uint32_t)std::min<size_t>(c->bins.cap, 0xFFFFFFFFu);
+  F.items = c->items.p;
+  F.item_cap = (uint32_t)std::min<size_t>(c->items.cap, 0xFFFFFFFFu);
   F.rgb8 = (outputs & MR_OUT_RGB8) ? c->rgb8.p : nullptr;
   F.depth = (outputs & MR_OUT_DEPTH) ? c->depth.p : nullptr;
   F.rgbf = (outputs & MR_OUT_RGB_F32) ? c->rgbf.p : nullptr;
@@ -525,24 +516,25 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   return launch_last(c);
 }
 
-// Waits for the last frame; re-runs it while the bin list overflowed.
+// Waits for the last frame; re-runs it while the large-triangle row-block
+// list overflowed.
 static int settle(mr_ctx* c) {
   if (!c->have_frame) return fail(c, MR_E_INVALID, "no frame rendered yet");
   for (int attempt = 0; attempt < 8; attempt++) {
     CK(cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "counter read");
     CK(cudaStreamSynchronize(c->stream), "frame wait");
-    if (!c->h_cnt->bin_overflow) {
+    if (!c->h_cnt->item_overflow) {
       c->pending = false;
       return (c->h_cnt->error_flags & 1u) ? fail(c, MR_E_BAD_INDEX, "a mesh index was out of range; those triangles were skipped") : MR_OK;
     }
-    size_t want = (size_t)c->h_cnt->bin_needed + c->h_cnt->bin_needed / 4 + 1024;
-    CK(c->bins.ensure(want), "bin buffer");
-    c->last.bins = c->bins.p;
-    c->last.bin_cap = (uint32_t)std::min<size_t>(c->bins.cap, 0xFFFFFFFFu);
+    size_t want = (size_t)c->h_cnt->item_count + c->h_cnt->item_count / 4 + 1024;
+    CK(c->items.ensure(want), "row-block buffer");
+    c->last.items = c->items.p;
+    c->last.item_cap = (uint32_t)std::min<size_t>(c->items.cap, 0xFFFFFFFFu);
     int rc = launch_last(c);
     if (rc) return rc;
   }
-  return fail(c, MR_E_NOMEM, "bin list kept overflowing");
+  return fail(c, MR_E_NOMEM, "row-block list kept overflowing");
 }
 
 MR_API int mr_read(mr_ctx* c, uint8_t* rgb8, float* depth, float* rgb_f32, uint32_t* tri_id, float* normals) {
@@ -604,7 +596,7 @@ MR_API int mr_get_stats(mr_ctx* c, mr_stats* s) {
   s->rasterised = (int64_t)k.rasterised;
   s->small_direct = (int64_t)k.small_direct;
   s->binned = (int64_t)k.rec_count;
-  s->bin_entries = (int64_t)k.bin_needed;
+  s->bin_entries = (int64_t)k.item_count;
   s->error_flags = k.error_flags;
   if (c->profiling) {
     s->n_stages = 5;
@@ -981,7 +973,7 @@ int batch_settle(mr_ctx* c, BatchSlot& B, cudaStream_t st) {
     int rc = batch_run(c, B, st, false, nullptr);
     if (rc) return rc;
   }
-  return fail(c, MR_E_NOMEM, "bin list kept overflowing");
+  return fail(c, MR_E_NOMEM, "row-block list kept overflowing");
 }
 
 MR_API int mr_read_batch(mr_ctx* c, int32_t s, uint8_t* rgb8, float* depth, uint32_t* ids) {

@@ -132,8 +132,7 @@ struct mr_ctx {
   DevBuf<float> depth, rgbf, normals, range;
   DevBuf<uint32_t> ids;
   DevBuf<BigRec> recs;
-  DevBuf<uint32_t> bins;
-  DevBuf<uint32_t> tiles;
+  DevBuf<LargeItem> items;     // large-triangle row blocks of the last frame
   // Per-frame staging, one block on both sides (one copy per frame):
   // renderables (cap) | tri, vertex and normal base tables 3 x (cap+1) | projection
   DevBuf<unsigned char> stage;

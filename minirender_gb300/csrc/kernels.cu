@@ -9,11 +9,11 @@
 //   k_setup        triangle assembly + near clip + triangle setup + cull;
 //                  small triangles rasterised by the warp that set them up,
 //                  one (triangle, row) per lane; large ones appended to a
-//                  warp-compacted record list       (src/Renderer.cpp:121-269, 351-379)
-//   k_bin_tile     one cooperative launch: screen-tile binning of the large
-//                  records (count, scan, scatter), then per-tile raster into a
-//                  shared-memory visibility tile merged into vis[] with
-//                  64-bit atomicMin                  (src/Renderer.cpp:238-269)
+//                  warp-compacted record list with their row blocks
+//                                                   (src/Renderer.cpp:121-269, 351-379)
+//   k_raster_large one warp per row block of a large sub-triangle (the setup
+//                  kernel lists the blocks), each row walked across the whole
+//                  bounding box with 64-bit atomicMin (src/Renderer.cpp:238-269)
 //   k_resolve      deferred pass: re-derives the winning sub-triangle's
 //                  barycentrics exactly, shades once per visible pixel and
 //                  writes RGB8/depth/ids            (src/Renderer.cpp:271-305, src/io.cpp:358-362)
@@ -688,9 +688,28 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
     unsigned base = 0;
     if (lane == 0) base = atomicAdd(&F.counters->rec_count, (unsigned)__popc(m));
     base = __shfl_sync(0xffffffffu, base, 0);
+    unsigned n_items = 0, slot = 0;
     if (kind[s] == 2) {
-      unsigned slot = base + __popc(m & lt);
-      if (slot < F.rec_cap) F.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
+      slot = base + __popc(m & lt);
+      if (slot < F.rec_cap) {
+        F.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
+        n_items = (unsigned)(S[s].y1 - S[s].y0 + kLargeRows) / kLargeRows;
+      }
+    }
+    // its row blocks: one range per warp, each lane's at its exclusive prefix
+    unsigned inc = n_items;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned u = __shfl_up_sync(0xffffffffu, inc, o);
+      if ((int)lane >= o) inc += u;
+    }
+    const unsigned total = __shfl_sync(0xffffffffu, inc, 31);
+    unsigned ibase = 0;
+    if (lane == 0 && total) ibase = atomicAdd(&F.counters->item_count, total);
+    ibase = __shfl_sync(0xffffffffu, ibase, 0) + inc - n_items;
+    for (unsigned k = 0; k < n_items; k++) {
+      if (ibase + k < F.item_cap) F.items[ibase + k] = LargeItem{slot, (uint32_t)(S[s].y0 + (int)k * kLargeRows)};
+      else F.counters->item_overflow = 1;
     }
   }
   raster_small(S, kind, g, 0u, FrameTarget{F.vis, F.v.W, persp}, s_rec[w], s_pre[w]);
@@ -700,109 +719,27 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
   block_flush(bc, &F.counters->rasterised, &F.counters->small_direct, &F.counters->clipped);
 }
 
-__device__ __forceinline__ void rec_tiles(int tile, const BigRec& B, int& tx0, int& ty0, int& tx1, int& ty1) {
-  tx0 = B.x0 / tile; tx1 = B.x1 / tile;
-  ty0 = B.y0 / tile; ty1 = B.y1 / tile;
-}
-
-// Rasterises the (record, row) pairs of records recs[bins[s..e)] that fall in
-// the tile at (px0, py0) into the shared-memory visibility tile svis (bins
-// null: records s..e directly).  Called by every thread of the block.
-__device__ __forceinline__ void raster_into_tile(const BigRec* recs, const uint32_t* bins, uint32_t s,
-                                                 uint32_t e, int TS, int px0, int py0, int px1, int py1,
-                                                 bool persp, unsigned long long* svis) {
-  const uint32_t work = (e - s) * (uint32_t)TS;
-  for (uint32_t i = threadIdx.x; i < work; i += blockDim.x) {
-    uint32_t ent = s + i / TS;
-    int y = py0 + (int)(i % TS);
-    BigRec B = recs[bins ? bins[ent] : ent];
-    if (y < B.y0 || y > B.y1 || y > py1) continue;
-    int xs = max(B.x0, px0), xe = min(B.x1, px1);
-    if (xs > xe) continue;
-    Setup S = rec_setup(B);
-    walk_row(S, persp, B.id, y, xs, xe, [&](int x, unsigned long long v, float, float) {
-      atomicMin(svis + (y - py0) * TS + (x - px0), v);
-    });
-  }
-}
-
-constexpr int kBinThreads = 256;
-
-// Screen-tile binning of the large records and their tile raster in one
-// cooperative launch (all blocks co-resident; grid-wide barriers between the
-// phases): count per tile -> exclusive scan -> scatter -> per-tile raster
-// merged into vis[].  With no large record every block returns at once,
-// before any barrier.
-__global__ void __launch_bounds__(kBinThreads) k_bin_tile(FrameParams F) {
+// Large sub-triangles, one warp per row block of kLargeRows rows of a record,
+// one row per lane: each row is walked across the record's whole bounding
+// box (no replay beyond the reference's own) with 64-bit atomicMin into
+// vis[] (src/Renderer.cpp:238-269).  An ordinary launch: with no large
+// record every warp leaves at once.
+__global__ void __launch_bounds__(256) k_raster_large(FrameParams F) {
+  pdl_wait();
   pdl_trigger();
-  extern __shared__ unsigned long long svis[];
-  __shared__ uint32_t part[kBinThreads];
-  const uint32_t nrec = min(F.counters->rec_count, F.rec_cap);
-  if (nrec == 0) return;
-  cg::grid_group grid = cg::this_grid();
-  const uint32_t gt = blockIdx.x * blockDim.x + threadIdx.x, gs = gridDim.x * blockDim.x;
-  const int ntiles = F.tiles_x * F.tiles_y;
-  const int TS = F.tile;
-  for (uint32_t i = gt; i < nrec; i += gs) {  // 1. count
-    int tx0, ty0, tx1, ty1;
-    rec_tiles(TS, F.recs[i], tx0, ty0, tx1, ty1);
-    for (int ty = ty0; ty <= ty1; ty++)
-      for (int tx = tx0; tx <= tx1; tx++) atomicAdd(F.tile_count + ty * F.tiles_x + tx, 1u);
-  }
-  grid.sync();
-  if (blockIdx.x == 0) {  // 2. exclusive scan, one block
-    int per = (ntiles + blockDim.x - 1) / blockDim.x;
-    int b = threadIdx.x * per, e = min(ntiles, b + per);
-    uint32_t sum = 0;
-    for (int i = b; i < e; i++) sum += F.tile_count[i];
-    part[threadIdx.x] = sum;
-    __syncthreads();
-    for (int off = 1; off < (int)blockDim.x; off <<= 1) {
-      uint32_t v = threadIdx.x >= (unsigned)off ? part[threadIdx.x - off] : 0;
-      __syncthreads();
-      part[threadIdx.x] += v;
-      __syncthreads();
-    }
-    uint32_t run = threadIdx.x ? part[threadIdx.x - 1] : 0;
-    for (int i = b; i < e; i++) {
-      F.tile_start[i] = run;
-      run += F.tile_count[i];
-    }
-    if (threadIdx.x == blockDim.x - 1) {
-      F.tile_start[ntiles] = part[blockDim.x - 1];
-      F.counters->bin_needed = part[blockDim.x - 1];
-      F.counters->bin_entries += part[blockDim.x - 1];
-    }
-  }
-  grid.sync();
-  for (uint32_t i = gt; i < nrec; i += gs) {  // 3. scatter
-    int tx0, ty0, tx1, ty1;
-    rec_tiles(TS, F.recs[i], tx0, ty0, tx1, ty1);
-    for (int ty = ty0; ty <= ty1; ty++)
-      for (int tx = tx0; tx <= tx1; tx++) {
-        int t = ty * F.tiles_x + tx;
-        uint32_t pos = F.tile_start[t] + atomicAdd(F.tile_fill + t, 1u);
-        if (pos < F.bin_cap) F.bins[pos] = i;
-        else F.counters->bin_overflow = 1;
-      }
-  }
-  grid.sync();
+  const uint32_t n = min(F.counters->item_count, F.item_cap);
   const bool persp = F.v.persp != 0;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {  // 4. raster
-    uint32_t s = F.tile_start[tile], e = min(F.tile_start[tile + 1], F.bin_cap);
-    if (s >= e) continue;  // uniform across the block
-    const int tx = tile % F.tiles_x, ty = tile / F.tiles_x;
-    const int px0 = tx * TS, py0 = ty * TS;
-    const int px1 = min(px0 + TS, F.v.W) - 1, py1 = min(py0 + TS, F.v.H) - 1;
-    for (int i = threadIdx.x; i < TS * TS; i += blockDim.x) svis[i] = VIS_EMPTY;
-    __syncthreads();
-    raster_into_tile(F.recs, F.bins, s, e, TS, px0, py0, px1, py1, persp, svis);
-    __syncthreads();
-    for (int i = threadIdx.x; i < TS * TS; i += blockDim.x) {
-      unsigned long long v = svis[i];
-      if (v != VIS_EMPTY) atomicMin(F.vis + (size_t)(py0 + i / TS) * F.v.W + (px0 + i % TS), v);
-    }
-    __syncthreads();
+  const int lane = (int)(threadIdx.x & 31);
+  const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n; it += nw) {
+    const LargeItem item = F.items[it];
+    const BigRec& R = F.recs[item.rec];
+    const int y = (int)item.row + lane;
+    if (y > R.y1) continue;
+    const Setup S = rec_setup(R);
+    unsigned long long* row = F.vis + (size_t)y * F.v.W;
+    walk_row(S, persp, R.id, y, S.x0, S.x1,
+             [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
   }
 }
 
@@ -1310,7 +1247,7 @@ static cudaError_t launch_coop(const void* fn, int grid, int block, void** args,
 
 // Launch sequence of one frame.  With F.g.va set, the vertex pass runs first
 // and the setup/resolve kernels read its buffers.  ev (optional, 6 events)
-// brackets the stages: clear+vertex, setup, binning+tile raster, -, resolve.
+// brackets the stages: clear+vertex, setup, large-triangle raster, -, resolve.
 cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev) {
   size_t npx = (size_t)F.v.W * F.v.H;
   const bool pre = F.g.va != nullptr;
@@ -1319,8 +1256,7 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   // kernel's atomics hit L2.
   int cgrid = grid_for(npx, 256);
   k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(
-      F.vis, npx, reinterpret_cast<uint32_t*>(F.counters), (uint32_t)(sizeof(Counters) / 4), F.tile_count,
-      (uint32_t)(3 * F.tiles_x * F.tiles_y + 1));
+      F.vis, npx, reinterpret_cast<uint32_t*>(F.counters), (uint32_t)(sizeof(Counters) / 4), nullptr, 0);
   // vertex pass, setup and resolve may be scheduled while their predecessor
   // finishes (they wait for it before reading its output)
   cudaError_t le = cudaSuccess;
@@ -1334,18 +1270,8 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
     if (le != cudaSuccess) return le;
   }
   if (ev) cudaEventRecord(ev[2], st);
-  {
-    static int per = 0;
-    const size_t smem = (size_t)32 * 32 * sizeof(unsigned long long);
-    if (!per) {
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bin_tile, kBinThreads, smem);
-      if (per <= 0) per = 1;
-    }
-    FrameParams Fc = F;
-    void* args[] = {&Fc};
-    cudaError_t e = launch_coop((const void*)k_bin_tile, sm_count() * per, kBinThreads, args, smem, st);
-    if (e != cudaSuccess) return e;
-  }
+  le = launch_after(k_raster_large, sm_count() * 8, 256, st, F);
+  if (le != cudaSuccess) return le;
   if (ev) cudaEventRecord(ev[3], st);
   if (ev) cudaEventRecord(ev[4], st);
   const int rgrid = ((F.v.W + kResolveTileW - 1) / kResolveTileW) * ((F.v.H + kResolveTileH - 1) / kResolveTileH);

@@ -89,22 +89,27 @@ struct Counters {
   unsigned int bin_needed;     // total (tile, record) pairs requested
   unsigned int bin_overflow;
   unsigned int work_next;      // persistent-kernel work counter
-  unsigned int pad[3];
+  unsigned int item_count;     // large-triangle row blocks requested (single frames)
+  unsigned int item_overflow;
+  unsigned int pad;
 };
 
 // One-frame launch.
+// Row block of a large sub-triangle: kLargeRows rows from `row` of record `rec`.
+struct LargeItem {
+  uint32_t rec, row;
+};
+constexpr int kLargeRows = 32;
+
 struct FrameParams {
   View v;
   Geo g;
-  int tile, tiles_x, tiles_y, small_max;
+  int small_max;
   unsigned long long* vis;    // W*H
-  BigRec* recs;
+  BigRec* recs;               // large sub-triangles
   uint32_t rec_cap;
-  uint32_t* tile_count;       // tiles_x*tiles_y (+1 scanned into tile_start)
-  uint32_t* tile_start;
-  uint32_t* tile_fill;
-  uint32_t* bins;
-  uint32_t bin_cap;
+  LargeItem* items;           // their row blocks
+  uint32_t item_cap;
   uint8_t* rgb8;
   float* depth;
   float* rgbf;

@@ -32,17 +32,12 @@ using namespace mrg;
 
 namespace {
 
-constexpr int kTile = 16;
-constexpr size_t kMaxTiles = 8704;  // >= ceil(W/16)*ceil(H/16) for W,H <= 4096, W*H <= 2^21
-
 constexpr size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
 constexpr size_t kVisOff = 0;
 constexpr size_t kVisBytes = (size_t)MR_NOALLOC_MAX_PIXELS * sizeof(unsigned long long);
 constexpr size_t kBadOff = al(kVisOff + kVisBytes);
 constexpr size_t kBadBytes = ((size_t)MR_NOALLOC_MAX_TRIANGLES / 32 + 1) * sizeof(uint32_t);
-constexpr size_t kTilesOff = al(kBadOff + kBadBytes);
-constexpr size_t kTilesBytes = (3 * kMaxTiles + 1) * sizeof(uint32_t);
-constexpr size_t kCntOff = al(kTilesOff + kTilesBytes);
+constexpr size_t kCntOff = al(kBadOff + kBadBytes);
 constexpr size_t kRsOff = al(kCntOff + sizeof(Counters));
 constexpr size_t kBaseOff = al(kRsOff + sizeof(DevRenderable));
 constexpr size_t kEnd = al(kBaseOff + 2 * sizeof(uint32_t));
@@ -133,7 +128,6 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   const uint32_t base[2] = {0, (uint32_t)M.n_tri};
 
   const int W = f->width, H = f->height;
-  const int tx = (W + kTile - 1) / kTile, ty = (H + kTile - 1) / kTile;
   FrameParams F;
   memset(&F, 0, sizeof(F));
   F.v.W = W;
@@ -153,23 +147,16 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   memcpy(F.v.bg, f->background, sizeof(F.v.bg));
   F.g.n_renderables = 1;
   F.g.n_tris = (uint32_t)M.n_tri;
-  F.tile = kTile;
-  F.tiles_x = tx;
-  F.tiles_y = ty;
   // Every sub-triangle is rasterised by the setup kernel itself, so no
-  // (data-dependent) record or bin storage is needed.
+  // (data-dependent) record or row-block storage is needed.
   F.small_max = 0x7fffffff;
   F.g.rs = (const DevRenderable*)(S + kRsOff);
   F.g.tri_base = (const uint32_t*)(S + kBaseOff);
   F.vis = (unsigned long long*)(S + kVisOff);
   F.recs = nullptr;
   F.rec_cap = 0;
-  uint32_t* tiles = (uint32_t*)(S + kTilesOff);
-  F.tile_count = tiles;
-  F.tile_fill = tiles + (size_t)tx * ty;
-  F.tile_start = tiles + (size_t)2 * tx * ty;
-  F.bins = nullptr;
-  F.bin_cap = 0;
+  F.items = nullptr;
+  F.item_cap = 0;
   F.rgb8 = rgb8;
   F.depth = depth;
   F.ids = tri_id;
@@ -178,7 +165,6 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   cudaError_t e = cudaMemcpyAsync(S + kRsOff, &R, sizeof(R), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemcpyAsync(S + kBaseOff, base, sizeof(base), cudaMemcpyHostToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(S + kCntOff, 0, sizeof(Counters), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(tiles, 0, sizeof(uint32_t) * ((size_t)3 * tx * ty + 1), st);
   if (e == cudaSuccess) e = launch_validate(M, (uint32_t*)(S + kBadOff), st);
   if (e == cudaSuccess) e = launch_frame(F, st, nullptr);
   Counters c;
