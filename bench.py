@@ -62,6 +62,8 @@ def parse():
     p.add_argument("--views", type=int, default=8, help="camera views per batched launch (config1-3)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs (profiling runs)")
+    p.add_argument("--e2e-contexts", type=int, default=3,
+                   help="contexts taking alternate end-to-end steps (frames in flight)")
     return p.parse_args()
 
 
@@ -246,44 +248,75 @@ KERNELS = {"clear+vertex": "k_clear+k_vertex", "setup": "k_setup", "large_raster
 
 def e2e_legs(args, ws, r, sc, st, flat, frame, rs, n, mesh_bytes, tex_bytes):
     """End-to-end frames/s through the C ABI with pinned host buffers: every
-    step copies the mesh and texture up, renders and reads RGB8 + depth back;
-    the second figure keeps the mesh resident and only reads back."""
-    import torch
-    from minirender_gb300 import scene as S
+    step copies the mesh and texture up, renders, and reads RGB8 + depth back
+    (mr_read_async).  `--e2e-contexts` contexts (default 3), each on its own
+    stream, take turns and share one upload stream (mr_set_upload_stream), so
+    one step's upload overlaps another's render and read-back; a context's
+    next render first completes its previous frame's read.  The
+    second figure keeps the mesh resident and only reads back."""
+    from minirender_gb300.renderer import Renderer
     mesh = flat.meshes[0]
-    pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory().numpy()  # noqa: E731
+    pin = lambda a: torch_pin(np.ascontiguousarray(a))  # noqa: E731
     pm, _keep = _pinned_copy(mesh)
     ptex = [pin(t) for t in flat.textures]
-    mh = r._mesh_handle(mesh)
-    th = [r._texture_handle(t) for t in flat.textures]
-    rgb8 = pin(np.empty((st.height, st.width, 3), np.uint8))
-    depth = pin(np.empty((st.height, st.width), np.float32))
+    extra = []
+    for _ in range(max(1, args.e2e_contexts) - 1):
+        r2 = Renderer(0)
+        r2.outputs = r.outputs
+        r2.state = st
+        r2.setScene(sc)
+        extra.append((r2,) + tuple(r2.prepare()))
+    lanes = []
+    for rr, fr, rsx, nx in [(r, frame, rs, n)] + extra:
+        lanes.append({"ctx": rr.ctx, "frame": fr, "rs": rsx, "n": nx, "mesh": rr._mesh_handle(mesh),
+                      "tex": [rr._texture_handle(t) for t in flat.textures],
+                      "rgb8": pin(np.empty((st.height, st.width, 3), np.uint8)),
+                      "depth": pin(np.empty((st.height, st.width), np.float32))})
     h2d = mesh_bytes + tex_bytes
-    d2h = rgb8.nbytes + depth.nbytes
+    d2h = lanes[0]["rgb8"].nbytes + lanes[0]["depth"].nbytes
+    # one upload stream for all contexts: their updates cross the host link
+    # one at a time, at its full rate, while the others render
+    import torch
+    up = torch.cuda.Stream()
+    for L in lanes:
+        L["ctx"].set_upload_stream(up.cuda_stream)
 
-    def e2e_step():
-        r.ctx.update_mesh(mh, pm.desc())
-        for h, t in zip(th, ptex):
-            r.ctx.update_texture(h, t)
-        r.ctx.render(frame, rs, n, r.outputs)
-        r.ctx.read_into(rgb8, depth)
+    def run(steps, upload):
+        for k in range(steps):
+            L = lanes[k % len(lanes)]
+            c = L["ctx"]
+            if upload:
+                c.update_mesh(L["mesh"], pm.desc())
+                for h, t in zip(L["tex"], ptex):
+                    c.update_texture(h, t)
+            c.render(L["frame"], L["rs"], L["n"], r.outputs)
+            c.read_async(L["rgb8"], L["depth"])
+        for L in lanes:
+            L["ctx"].wait()
 
-    for _ in range(2):
-        e2e_step()
-    barrier(ws)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        e2e_step()
-    e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
-    e2e_value = args.steps * ws / e2e_s
-    # resident variant: only the camera changes per frame
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r.ctx.render(frame, rs, n, r.outputs)
-        r.ctx.read_into(rgb8, depth)
-    res_s = max_over_ranks(time.perf_counter() - t0, ws)
-    return e2e_value, args.steps * ws / res_s, h2d, d2h
+    try:
+        run(4, True)
+        barrier(ws)
+        t0 = time.perf_counter()
+        run(args.steps, True)
+        e2e_s = max_over_ranks(time.perf_counter() - t0, ws)
+        # resident variant: only the camera changes per frame
+        run(4, False)
+        t0 = time.perf_counter()
+        run(args.steps, False)
+        res_s = max_over_ranks(time.perf_counter() - t0, ws)
+    finally:
+        for L in lanes:
+            L["ctx"].set_upload_stream(None)
+        for x in extra:
+            x[0].close()
+    return args.steps * ws / e2e_s, args.steps * ws / res_s, h2d, d2h
 
+
+def torch_pin(a: np.ndarray) -> np.ndarray:
+    """A pinned host copy of `a` (page-locked through torch's host allocator)."""
+    import torch
+    return torch.from_numpy(a).pin_memory().numpy()
 
 
 def scene_tris(sc) -> int:
@@ -704,7 +737,8 @@ def gpu_arm(args, ws, rank, local):
         "mtri_per_s": round(value * T / 1e6, 2),
         "e2e": None if e2e_value is None else {
             "value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": int(h2d),
-            "d2h_bytes_per_step": int(d2h)},
+            "d2h_bytes_per_step": int(d2h), "contexts": max(1, args.e2e_contexts),
+            "link_gbs": round((h2d + d2h) * e2e_value / ws / 1e9, 1)},
         "e2e_resident_mesh": None if res_value is None else {
             "value": round(res_value, 3), "unit": UNIT, "h2d_bytes_per_step": 0,
             "d2h_bytes_per_step": int(d2h)},

@@ -161,6 +161,13 @@ MR_API int mr_destroy(mr_ctx* ctx);
 /* cudaStream_t passed as void*; NULL = the context's own stream. */
 MR_API int mr_set_stream(mr_ctx* ctx, void* cuda_stream);
 MR_API int mr_synchronize(mr_ctx* ctx);
+/* Stream for mr_mesh_update / mr_texture_update (NULL: the context's own
+ * stream).  An update waits on the device for the frames already queued on
+ * the context (they read the old contents); the next frame waits for the
+ * update.  Contexts that share one upload stream send their updates over
+ * the host link one at a time, each at the link's full rate, while their
+ * frames render on their own streams. */
+MR_API int mr_set_upload_stream(mr_ctx* ctx, void* cuda_stream);
 /* Small-triangle bounding-box limit (pixels) of mr_render.  `tile` (8, 16
  * or 32) is validated and kept for source compatibility; single frames no
  * longer bin into tiles. */
@@ -196,6 +203,15 @@ MR_API int mr_render(mr_ctx* ctx, const mr_frame* frame, const mr_renderable* re
  * outputs of the last frame to host memory (NULL = skip) and waits. */
 MR_API int mr_read(mr_ctx* ctx, uint8_t* rgb8, float* depth, float* rgb_f32, uint32_t* tri_id,
                    float* normals);
+/* mr_read without the wait: queues the copies of the last frame's outputs
+ * (pinned host buffers make them asynchronous) and returns.  mr_wait -- or
+ * the next mr_read / mr_render / mr_get_stats on this context -- completes
+ * them; the buffers must stay valid until then.  Several contexts, each on
+ * its own stream, keep frames in flight: one context's upload and render
+ * overlap another's read-back (see mr_set_upload_stream). */
+MR_API int mr_read_async(mr_ctx* ctx, uint8_t* rgb8, float* depth, float* rgb_f32, uint32_t* tri_id,
+                         float* normals);
+MR_API int mr_wait(mr_ctx* ctx);
 MR_API int mr_get_outputs(mr_ctx* ctx, mr_outputs* out);
 MR_API int mr_get_stats(mr_ctx* ctx, mr_stats* out);
 /* Replaces: Renderer::getRangeImage (src/Renderer.cpp:388-415): view-space

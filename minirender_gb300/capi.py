@@ -28,6 +28,7 @@ _SIGS = {
     "mr_destroy": ([_P], C.c_int),
     "mr_set_stream": ([_P, _P], C.c_int),
     "mr_synchronize": ([_P], C.c_int),
+    "mr_set_upload_stream": ([_P, _P], C.c_int),
     "mr_set_tuning": ([_P, C.c_int, C.c_int], C.c_int),
     "mr_set_profiling": ([_P, C.c_int], C.c_int),
     "mr_mesh_upload": ([_P, C.POINTER(abi.mr_mesh_desc), C.POINTER(_I)], C.c_int),
@@ -39,6 +40,8 @@ _SIGS = {
     "mr_texture_free": ([_P, _I], C.c_int),
     "mr_render": ([_P, C.POINTER(abi.mr_frame), _P, _I, _I], C.c_int),
     "mr_read": ([_P, _P, _P, _P, _P, _P], C.c_int),
+    "mr_read_async": ([_P, _P, _P, _P, _P, _P], C.c_int),
+    "mr_wait": ([_P], C.c_int),
     "mr_get_outputs": ([_P, C.POINTER(abi.mr_outputs)], C.c_int),
     "mr_get_stats": ([_P, C.POINTER(abi.mr_stats)], C.c_int),
     "mr_read_range_image": ([_P, _P], C.c_int),
@@ -143,6 +146,10 @@ class Context:
     def set_stream(self, stream_ptr: int):
         self._check(lib().mr_set_stream(self.h, stream_ptr), "mr_set_stream")
 
+    def set_upload_stream(self, stream_ptr: Optional[int]):
+        """Stream for mesh / texture updates (None: the context's own)."""
+        self._check(lib().mr_set_upload_stream(self.h, stream_ptr), "mr_set_upload_stream")
+
     def synchronize(self):
         self._check(lib().mr_synchronize(self.h), "mr_synchronize")
 
@@ -206,6 +213,22 @@ class Context:
     def read_into(self, rgb8: Optional[np.ndarray], depth: Optional[np.ndarray]) -> None:
         """D2H of RGB8 and depth into caller-owned (e.g. pinned) arrays."""
         self._check(lib().mr_read(self.h, _ptr(rgb8), _ptr(depth), None, None, None), "mr_read")
+
+    def read_async(self, rgb8: Optional[np.ndarray], depth: Optional[np.ndarray],
+                   tri_id: Optional[np.ndarray] = None) -> None:
+        """Queues the D2H of RGB8, depth (and triangle ids) into caller-owned
+        (pinned, for an asynchronous copy) arrays; wait() -- or the next
+        read, render or stats call -- completes it."""
+        self._check(lib().mr_read_async(self.h, _ptr(rgb8), _ptr(depth), None, _ptr(tri_id), None),
+                    "mr_read_async")
+
+    def wait(self) -> int:
+        """Completes the last frame and any queued reads; returns 0 or
+        MR_E_BAD_INDEX (raises on other errors)."""
+        rc = lib().mr_wait(self.h)
+        if rc not in (0, abi.MR_E_BAD_INDEX):
+            self._check(rc, "mr_wait")
+        return rc
 
     def range_image(self) -> np.ndarray:
         H, W = self._frame_hw

@@ -50,6 +50,9 @@ MR_API int mr_create(int device, mr_ctx** out) {
   if (e == cudaSuccess) e = cudaMallocHost(&c->h_cnt, sizeof(Counters));
   for (int i = 0; i < 8 && e == cudaSuccess; i++) e = cudaEventCreate(&c->ev[i]);
   if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->staged, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->read_done, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->compute_mark, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->uploaded, cudaEventDisableTiming);
 
   if (e != cudaSuccess) {
     delete c;
@@ -65,6 +68,7 @@ MR_API int mr_destroy(mr_ctx* c) {
   {
     std::lock_guard<std::recursive_mutex> g(c->mu);
     cudaSetDevice(c->device);
+    if (c->upload_waiting) cudaEventSynchronize(c->uploaded);
     cudaStreamSynchronize(c->stream);
     for (auto& m : c->meshes)
       if (m.mem) cudaFree(m.mem);
@@ -72,7 +76,7 @@ MR_API int mr_destroy(mr_ctx* c) {
       if (t.mem) cudaFree(t.mem);
     c->vis.release(); c->rgb8.release(); c->depth.release(); c->rgbf.release();
     c->normals.release(); c->range.release(); c->ids.release(); c->recs.release();
-    c->items.release(); c->stage.release();
+    c->items.release(); c->spill.release(); c->stage.release();
     c->va.release(); c->vb.release(); c->vn.release();
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->d_cnt) cudaFree(c->d_cnt);
@@ -80,6 +84,9 @@ MR_API int mr_destroy(mr_ctx* c) {
     for (auto& e : c->ev)
       if (e) cudaEventDestroy(e);
     if (c->staged) cudaEventDestroy(c->staged);
+    if (c->read_done) cudaEventDestroy(c->read_done);
+    if (c->compute_mark) cudaEventDestroy(c->compute_mark);
+    if (c->uploaded) cudaEventDestroy(c->uploaded);
     c->b.release();
     if (c->own) cudaStreamDestroy(c->own);
   }
@@ -87,10 +94,55 @@ MR_API int mr_destroy(mr_ctx* c) {
   return MR_OK;
 }
 
+// The compute stream waits (on the device) for the last update issued on the
+// upload stream.
+static int join_upload(mr_ctx* c) {
+  if (!c->upload_waiting) return MR_OK;
+  CK(cudaStreamWaitEvent(c->stream, c->uploaded, 0), "upload wait");
+  c->upload_waiting = false;
+  for (auto& m : c->meshes)
+    if (m.live && m.validate_pending) {
+      CK(launch_validate(m.d, (uint32_t*)m.d.bad, c->stream), "validate launch");
+      m.validate_pending = false;
+    }
+  return MR_OK;
+}
+
+// Stream for a mesh or texture update: the upload stream, after everything
+// queued so far on the compute stream (frames that read the old contents);
+// without one, the compute stream itself.
+static cudaStream_t begin_update(mr_ctx* c) {
+  if (!c->upload) return c->stream;
+  if (cudaEventRecord(c->compute_mark, c->stream) != cudaSuccess ||
+      cudaStreamWaitEvent(c->upload, c->compute_mark, 0) != cudaSuccess)
+    return nullptr;
+  return c->upload;
+}
+
+static int end_update(mr_ctx* c) {
+  if (!c->upload) return MR_OK;
+  CK(cudaEventRecord(c->uploaded, c->upload), "upload event");
+  c->upload_waiting = true;
+  return MR_OK;
+}
+
 MR_API int mr_set_stream(mr_ctx* c, void* s) {
   if (!c) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  int rc = join_upload(c);
+  if (rc) return rc;
   c->stream = s ? (cudaStream_t)s : c->own;
+  return MR_OK;
+}
+
+MR_API int mr_set_upload_stream(mr_ctx* c, void* s) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  int rc = join_upload(c);
+  if (rc) return rc;
+  c->upload = (cudaStream_t)s;
   return MR_OK;
 }
 
@@ -98,6 +150,8 @@ MR_API int mr_synchronize(mr_ctx* c) {
   if (!c) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
   cudaSetDevice(c->device);
+  int rc = join_upload(c);
+  if (rc) return rc;
   CK(cudaStreamSynchronize(c->stream), "cudaStreamSynchronize");
   return MR_OK;
 }
@@ -119,6 +173,9 @@ MR_API int mr_set_profiling(mr_ctx* c, int on) {
   return MR_OK;
 }
 
+// Copies the mesh arrays on st and checks the indices there, or -- when st
+// is the upload stream, which carries copies only so the next update never
+// waits for SMs -- on the compute stream once the next frame joins it.
 static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t st) {
   DevMesh& M = m.d;
   char* base = (char*)m.mem;
@@ -149,7 +206,8 @@ static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t 
     if (M.has_uv && !t_alias)
       CK(cudaMemcpyAsync((void*)M.tidx, d->texcoordsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
   }
-  CK(launch_validate(M, (uint32_t*)M.bad, st), "validate launch");
+  if (c->upload && st == c->upload) m.validate_pending = true;
+  else CK(launch_validate(M, (uint32_t*)M.bad, st), "validate launch");
   return MR_OK;
 }
 
@@ -224,6 +282,7 @@ int mesh_destroy(mr_ctx* c, int32_t h, cudaStream_t stream) {
   if (stream) {
     CK(cudaFreeAsync(m.mem, stream), "mesh free");
   } else {
+    join_upload(c);
     cudaStreamSynchronize(c->stream);
     if (m.stream_ordered) cudaDeviceSynchronize();
     cudaFree(m.mem);
@@ -254,7 +313,11 @@ MR_API int mr_mesh_update(mr_ctx* c, int32_t h, const mr_mesh_desc* d) {
       (has_uv && (d->texcoordsI == d->indices) != (m.d.tidx == m.d.idx)))
     return fail(c, MR_E_INVALID, "mr_mesh_update needs normalsI / texcoordsI shared with indices as at upload");
   cudaSetDevice(c->device);
-  return copy_mesh(c, m, d, c->stream);
+  cudaStream_t st = begin_update(c);
+  if (!st) return fail(c, MR_E_CUDA, "upload stream ordering failed");
+  rc = copy_mesh(c, m, d, st);
+  if (rc) return rc;
+  return end_update(c);
 }
 
 MR_API int mr_mesh_free(mr_ctx* c, int32_t h) {
@@ -304,6 +367,7 @@ int texture_destroy(mr_ctx* c, int32_t h, cudaStream_t stream) {
   if (stream) {
     CK(cudaFreeAsync(t.mem, stream), "texture free");
   } else {
+    join_upload(c);
     cudaStreamSynchronize(c->stream);
     if (t.stream_ordered) cudaDeviceSynchronize();
     cudaFree(t.mem);
@@ -336,8 +400,10 @@ MR_API int mr_texture_update(mr_ctx* c, int32_t h, const void* texels) {
   const TexRec& t = c->textures[h];
   size_t bytes = (size_t)t.rows * t.cols * (t.rgb8 ? 3 : 12);
   cudaSetDevice(c->device);
-  CK(cudaMemcpyAsync(t.mem, texels, bytes, cudaMemcpyHostToDevice, c->stream), "texture copy");
-  return MR_OK;
+  cudaStream_t st = begin_update(c);
+  if (!st) return fail(c, MR_E_CUDA, "upload stream ordering failed");
+  CK(cudaMemcpyAsync(t.mem, texels, bytes, cudaMemcpyHostToDevice, st), "texture copy");
+  return end_update(c);
 }
 
 MR_API int mr_texture_free(mr_ctx* c, int32_t h) {
@@ -347,12 +413,14 @@ MR_API int mr_texture_free(mr_ctx* c, int32_t h) {
   return texture_destroy(c, h, nullptr);
 }
 
+static int settle(mr_ctx* c);
+
 // Launches the kernels of c->last after resetting the per-frame counters.
 static int launch_last(mr_ctx* c) {
   FrameParams& F = c->last;
   cudaStream_t st = c->stream;
   // (the clear kernel also zeroes the counters and the tile tables)
-  CK(launch_frame(F, st, c->profiling ? c->ev : nullptr), "frame launch");
+  CK(launch_frame(F, st, c->profiling ? c->ev : nullptr, c->staged), "frame launch");
   return MR_OK;
 }
 
@@ -364,6 +432,14 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
       f->width > (1 << 16) || f->height > (1 << 16))
     return fail(c, MR_E_INVALID, "frame size out of range");
   cudaSetDevice(c->device);
+  if (c->async_read) {  // the last frame's reads complete before it is replaced
+    int rc = settle(c);
+    if (rc && rc != MR_E_BAD_INDEX) return rc;
+  }
+  {
+    int rc = join_upload(c);
+    if (rc) return rc;
+  }
   // Per-renderable matrices and materials, Renderer::paintMesh (src/Renderer.cpp:336-338).
   uint64_t total = 0;
   for (int32_t i = 0; i < n; i++) {
@@ -387,8 +463,9 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     c->h_rs_cap = 0;
     c->off_bases = align256(sizeof(DevRenderable) * nrs);
     c->off_P = c->off_bases + align256(sizeof(uint32_t) * 3 * (nrs + 1));
-    c->stage_bytes = c->off_P + sizeof(float) * 16;
+    c->stage_bytes = (c->off_P + sizeof(float) * 16 + 15) & ~(size_t)15;
     CK(cudaMallocHost(&c->h_stage, c->stage_bytes), "pinned staging");
+    CK(cudaHostGetDevicePointer((void**)&c->d_stage_src, c->h_stage, 0), "mapped staging");
     CK(c->stage.ensure(c->stage_bytes), "staging buffer");
     c->h_rs = (DevRenderable*)c->h_stage;
     c->h_tri_base = (uint32_t*)(c->h_stage + c->off_bases);
@@ -453,6 +530,7 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   if (outputs & MR_OUT_TRI_ID) CK(c->ids.ensure(npx), "id buffer");
   if (f->save_normals) CK(c->normals.ensure(3 * npx), "normals buffer");
   CK(c->recs.ensure((size_t)2 * total), "record buffer");
+  CK(c->spill.ensure((size_t)2 * total), "spill buffer");
   if (c->items.cap < ((size_t)1 << 18)) CK(c->items.ensure((size_t)1 << 18), "row-block buffer");
   // The per-vertex pass pays off when vertices are shared (each one used by
   // two or more triangle corners on average); for triangle soups every
@@ -464,11 +542,13 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     CK(c->vn.ensure(nbase), "normal buffer");
   }
   memcpy(c->h_P, f->projection, sizeof(float) * 16);
-  CK(cudaMemcpyAsync(c->stage.p, c->h_stage, c->stage_bytes, cudaMemcpyHostToDevice, c->stream), "staging upload");
-  CK(cudaEventRecord(c->staged, c->stream), "staging event");
 
   FrameParams& F = c->last;
   memset(&F, 0, sizeof(F));
+  // the clear kernel fetches the staging block from mapped pinned memory
+  F.stage_src = (const uint4*)c->d_stage_src;
+  F.stage_dst = (uint4*)c->stage.p;
+  F.stage_n16 = (uint32_t)(c->stage_bytes / 16);
   F.v.W = W;
   F.v.H = H;
   F.v.w = (float)W;
@@ -503,6 +583,7 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   F.rec_cap = (uint32_t)std::min<size_t>(c->recs.cap, 0xFFFFFFFFu);
   F.items = c->items.p;
   F.item_cap = (uint32_t)std::min<size_t>(c->items.cap, 0xFFFFFFFFu);
+  F.spill = c->spill.p;
   F.rgb8 = (outputs & MR_OUT_RGB8) ? c->rgb8.p : nullptr;
   F.depth = (outputs & MR_OUT_DEPTH) ? c->depth.p : nullptr;
   F.rgbf = (outputs & MR_OUT_RGB_F32) ? c->rgbf.p : nullptr;
@@ -516,57 +597,95 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   return launch_last(c);
 }
 
-// Waits for the last frame; re-runs it while the large-triangle row-block
-// list overflowed.
+// Queues the device-to-host copies of the last frame's outputs (null
+// pointers are skipped) on the context's stream.
+static int queue_reads(mr_ctx* c, const ReadTargets& r) {
+  size_t npx = (size_t)c->last.v.W * c->last.v.H;
+  cudaStream_t st = c->stream;
+  if (r.rgb8) CK(cudaMemcpyAsync(r.rgb8, c->last.rgb8, 3 * npx, cudaMemcpyDeviceToHost, st), "rgb8 read");
+  if (r.depth) CK(cudaMemcpyAsync(r.depth, c->last.depth, 4 * npx, cudaMemcpyDeviceToHost, st), "depth read");
+  if (r.rgbf) CK(cudaMemcpyAsync(r.rgbf, c->last.rgbf, 12 * npx, cudaMemcpyDeviceToHost, st), "rgb read");
+  if (r.ids) CK(cudaMemcpyAsync(r.ids, c->last.ids, 4 * npx, cudaMemcpyDeviceToHost, st), "id read");
+  if (r.normals) CK(cudaMemcpyAsync(r.normals, c->last.normals, 12 * npx, cudaMemcpyDeviceToHost, st), "normals read");
+  return MR_OK;
+}
+
+// Waits for the last frame and reads its counters.  An outstanding
+// mr_read_async completes here: its counter copy was queued behind the frame
+// and its output copies before the read_done event (work queued on the
+// stream after them, such as the next frame's mesh upload, is not waited
+// for).  A frame whose row blocks overflowed the list was still rasterised
+// completely (through the spill list); the list grows for the next frames.
 static int settle(mr_ctx* c) {
   if (!c->have_frame) return fail(c, MR_E_INVALID, "no frame rendered yet");
-  for (int attempt = 0; attempt < 8; attempt++) {
+  if (c->async_read) {
+    CK(cudaEventSynchronize(c->read_done), "read wait");
+    c->async_read = false;
+  } else {
     CK(cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "counter read");
     CK(cudaStreamSynchronize(c->stream), "frame wait");
-    if (!c->h_cnt->item_overflow) {
-      c->pending = false;
-      return (c->h_cnt->error_flags & 1u) ? fail(c, MR_E_BAD_INDEX, "a mesh index was out of range; those triangles were skipped") : MR_OK;
-    }
-    size_t want = (size_t)c->h_cnt->item_count + c->h_cnt->item_count / 4 + 1024;
-    CK(c->items.ensure(want), "row-block buffer");
-    c->last.items = c->items.p;
-    c->last.item_cap = (uint32_t)std::min<size_t>(c->items.cap, 0xFFFFFFFFu);
-    int rc = launch_last(c);
-    if (rc) return rc;
   }
-  return fail(c, MR_E_NOMEM, "row-block list kept overflowing");
+  c->pending = false;
+  const Counters& k = *c->h_cnt;
+  if (k.item_count > c->last.item_cap) {
+    size_t want = (size_t)k.item_count + k.item_count / 4 + 1024;
+    CK(c->items.ensure(want), "row-block buffer");
+  }
+  return (k.error_flags & 1u) ? fail(c, MR_E_BAD_INDEX, "a mesh index was out of range; those triangles were skipped") : MR_OK;
+}
+
+static int check_reads(mr_ctx* c, const ReadTargets& r) {
+  if (!c->have_frame) return fail(c, MR_E_INVALID, "no frame rendered yet");
+  if (r.rgb8 && !c->last.rgb8) return fail(c, MR_E_INVALID, "rgb8 was not requested for this frame");
+  if (r.depth && !c->last.depth) return fail(c, MR_E_INVALID, "depth was not requested for this frame");
+  if (r.rgbf && !c->last.rgbf) return fail(c, MR_E_INVALID, "float image was not requested for this frame");
+  if (r.ids && !c->last.ids) return fail(c, MR_E_INVALID, "ids were not requested for this frame");
+  if (r.normals && !c->last.normals) return fail(c, MR_E_INVALID, "normals were not requested for this frame");
+  return MR_OK;
 }
 
 MR_API int mr_read(mr_ctx* c, uint8_t* rgb8, float* depth, float* rgb_f32, uint32_t* tri_id, float* normals) {
   if (!c) return MR_E_INVALID;
   std::lock_guard<std::recursive_mutex> g(c->mu);
   cudaSetDevice(c->device);
-  int rc = settle(c);
+  const ReadTargets r{rgb8, depth, rgb_f32, tri_id, normals};
+  int rc = check_reads(c, r);
+  if (rc) return rc;
+  rc = settle(c);
   if (rc && rc != MR_E_BAD_INDEX) return rc;
-  size_t npx = (size_t)c->last.v.W * c->last.v.H;
-  cudaStream_t st = c->stream;
-  if (rgb8) {
-    if (!c->last.rgb8) return fail(c, MR_E_INVALID, "rgb8 was not requested for this frame");
-    CK(cudaMemcpyAsync(rgb8, c->last.rgb8, 3 * npx, cudaMemcpyDeviceToHost, st), "rgb8 read");
-  }
-  if (depth) {
-    if (!c->last.depth) return fail(c, MR_E_INVALID, "depth was not requested for this frame");
-    CK(cudaMemcpyAsync(depth, c->last.depth, 4 * npx, cudaMemcpyDeviceToHost, st), "depth read");
-  }
-  if (rgb_f32) {
-    if (!c->last.rgbf) return fail(c, MR_E_INVALID, "float image was not requested for this frame");
-    CK(cudaMemcpyAsync(rgb_f32, c->last.rgbf, 12 * npx, cudaMemcpyDeviceToHost, st), "rgb read");
-  }
-  if (tri_id) {
-    if (!c->last.ids) return fail(c, MR_E_INVALID, "ids were not requested for this frame");
-    CK(cudaMemcpyAsync(tri_id, c->last.ids, 4 * npx, cudaMemcpyDeviceToHost, st), "id read");
-  }
-  if (normals) {
-    if (!c->last.normals) return fail(c, MR_E_INVALID, "normals were not requested for this frame");
-    CK(cudaMemcpyAsync(normals, c->last.normals, 12 * npx, cudaMemcpyDeviceToHost, st), "normals read");
-  }
-  CK(cudaStreamSynchronize(st), "read wait");
+  int q = queue_reads(c, r);
+  if (q) return q;
+  CK(cudaStreamSynchronize(c->stream), "read wait");
   return rc;
+}
+
+MR_API int mr_read_async(mr_ctx* c, uint8_t* rgb8, float* depth, float* rgb_f32, uint32_t* tri_id, float* normals) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  const ReadTargets r{rgb8, depth, rgb_f32, tri_id, normals};
+  int rc = check_reads(c, r);
+  if (rc) return rc;
+  if (c->async_read) {  // an earlier read of this frame still outstanding
+    rc = settle(c);
+    if (rc && rc != MR_E_BAD_INDEX) return rc;
+  }
+  if (c->pending)
+    CK(cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(Counters), cudaMemcpyDeviceToHost, c->stream), "counter read");
+  int q = queue_reads(c, r);
+  if (q) return q;
+  CK(cudaEventRecord(c->read_done, c->stream), "read event");
+  c->async_read = true;
+  return MR_OK;
+}
+
+MR_API int mr_wait(mr_ctx* c) {
+  if (!c) return MR_E_INVALID;
+  std::lock_guard<std::recursive_mutex> g(c->mu);
+  cudaSetDevice(c->device);
+  if (c->have_frame && (c->pending || c->async_read)) return settle(c);
+  CK(cudaStreamSynchronize(c->stream), "wait");
+  return MR_OK;
 }
 
 MR_API int mr_get_outputs(mr_ctx* c, mr_outputs* o) {
@@ -949,7 +1068,9 @@ MR_API int mr_render_batch(mr_ctx* c, const mr_batch_scene* sc, int32_t n_scenes
   std::lock_guard<std::recursive_mutex> g(c->mu);
   cudaSetDevice(c->device);
   BatchSlot& B = c->b;
-  int rc = batch_stage(c, B, sc, n_scenes, rs, n_rs, outputs);
+  int rc = join_upload(c);
+  if (rc) return rc;
+  rc = batch_stage(c, B, sc, n_scenes, rs, n_rs, outputs);
   if (rc) return rc;
   rc = batch_run(c, B, c->stream, c->profiling, c->ev);
   if (rc) return rc;

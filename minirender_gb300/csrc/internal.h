@@ -15,7 +15,7 @@
 
 namespace mrg {
 cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st);
-cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev);
+cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev, cudaEvent_t staged = nullptr);
 cudaError_t launch_range(int W, int H, const float* dP, const float* depth, float* xyz,
                          cudaStream_t st);
 cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* block_sums, cudaStream_t st,
@@ -39,6 +39,7 @@ struct MeshRec {
   size_t bytes = 0;
   DevMesh d{};
   int32_t n_idx = 0;
+  bool validate_pending = false;  // updated on the upload stream, indices not yet checked
 };
 
 struct TexRec {
@@ -120,6 +121,15 @@ struct BatchSlot {
   void release();
 };
 
+// Host destinations of one frame's reads (null: not read).
+struct ReadTargets {
+  uint8_t* rgb8;
+  float* depth;
+  float* rgbf;
+  uint32_t* ids;
+  float* normals;
+};
+
 struct mr_ctx {
   int device = 0;
   cudaStream_t own = nullptr;
@@ -133,10 +143,12 @@ struct mr_ctx {
   DevBuf<uint32_t> ids;
   DevBuf<BigRec> recs;
   DevBuf<LargeItem> items;     // large-triangle row blocks of the last frame
+  DevBuf<LargeItem> spill;     // records whose rows did not fit items (one entry each)
   // Per-frame staging, one block on both sides (one copy per frame):
   // renderables (cap) | tri, vertex and normal base tables 3 x (cap+1) | projection
   DevBuf<unsigned char> stage;
   unsigned char* h_stage = nullptr;
+  unsigned char* d_stage_src = nullptr;  // h_stage as the device sees it (mapped)
   size_t h_rs_cap = 0, stage_bytes = 0, off_bases = 0, off_P = 0;
   DevRenderable* h_rs = nullptr;
   uint32_t* h_tri_base = nullptr;
@@ -147,11 +159,16 @@ struct mr_ctx {
   Counters* h_cnt = nullptr;
   cudaEvent_t ev[8] = {};
   cudaEvent_t staged = nullptr;
+  cudaEvent_t read_done = nullptr;  // after the copies of the last mr_read_async
+  cudaStream_t upload = nullptr;     // mesh / texture updates (null: the compute stream)
+  cudaEvent_t compute_mark = nullptr, uploaded = nullptr;
+  bool upload_waiting = false;       // the compute stream has not yet waited for `uploaded`
   bool profiling = false;
   int tile = 16;
   int small_max = 64;
   bool have_frame = false;
   bool pending = false;  // a frame was launched and not yet checked
+  bool async_read = false;  // mr_read_async copies queued, not yet waited for
   FrameParams last{};
   mr_frame last_frame{};
   int outputs = 0;

@@ -492,10 +492,15 @@ __device__ __forceinline__ uint8_t to_byte(float v) { return (uint8_t)(int)clamp
 // ------------------------------------------------------------------ kernels
 // vis[0..n) = VIS_EMPTY; also zeroes z[0..nz) (a frame's counters and tile
 // tables, so they need no separate memset before the frame).
-__global__ void k_clear(unsigned long long* vis, size_t n, uint32_t* z0, uint32_t nz0, uint32_t* z1, uint32_t nz1) {
+// With src, also copies n16 16-byte units from src (mapped pinned host
+// memory: the frame's staging block) to dst, so a frame never queues behind
+// other streams' transfers on the copy engine.
+__global__ void k_clear(unsigned long long* vis, size_t n, uint32_t* z0, uint32_t nz0, uint32_t* z1, uint32_t nz1,
+                        const uint4* src, uint4* dst, uint32_t n16) {
   pdl_trigger();
   size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t k = i; k < n16; k += stride) dst[k] = src[k];
   for (size_t k = i; k < nz0; k += stride) z0[k] = 0;
   for (size_t k = i; k < nz1; k += stride) z1[k] = 0;
   for (; i < n; i += stride) vis[i] = VIS_EMPTY;
@@ -707,9 +712,16 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
     unsigned ibase = 0;
     if (lane == 0 && total) ibase = atomicAdd(&F.counters->item_count, total);
     ibase = __shfl_sync(0xffffffffu, ibase, 0) + inc - n_items;
+    // blocks past the end of the list: the record's remaining rows go to the
+    // spill list (at most one entry per record, so it cannot overflow)
     for (unsigned k = 0; k < n_items; k++) {
-      if (ibase + k < F.item_cap) F.items[ibase + k] = LargeItem{slot, (uint32_t)(S[s].y0 + (int)k * kLargeRows)};
-      else F.counters->item_overflow = 1;
+      const uint32_t row = (uint32_t)(S[s].y0 + (int)k * kLargeRows);
+      if (ibase + k < F.item_cap) {
+        F.items[ibase + k] = LargeItem{slot, row};
+      } else {
+        F.spill[atomicAdd(&F.counters->spill_count, 1u)] = LargeItem{slot, row};
+        break;
+      }
     }
   }
   raster_small(S, kind, g, 0u, FrameTarget{F.vis, F.v.W, persp}, s_rec[w], s_pre[w]);
@@ -722,24 +734,35 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
 // Large sub-triangles, one warp per row block of kLargeRows rows of a record,
 // one row per lane: each row is walked across the record's whole bounding
 // box (no replay beyond the reference's own) with 64-bit atomicMin into
-// vis[] (src/Renderer.cpp:238-269).  An ordinary launch: with no large
-// record every warp leaves at once.
+// vis[] (src/Renderer.cpp:238-269).  Then the spill list: one warp per
+// record, its remaining rows kLargeRows at a time.  An ordinary launch: with
+// no large record every warp leaves at once.
+__device__ __forceinline__ void raster_rec_row(const FrameParams& F, bool persp, const BigRec& R, int y) {
+  const Setup S = rec_setup(R);
+  unsigned long long* row = F.vis + (size_t)y * F.v.W;
+  walk_row(S, persp, R.id, y, S.x0, S.x1,
+           [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
+}
+
 __global__ void __launch_bounds__(256) k_raster_large(FrameParams F) {
   pdl_wait();
   pdl_trigger();
   const uint32_t n = min(F.counters->item_count, F.item_cap);
+  const uint32_t n_spill = F.counters->spill_count;
   const bool persp = F.v.persp != 0;
   const int lane = (int)(threadIdx.x & 31);
   const uint32_t nw = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t it = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < n; it += nw) {
+  const uint32_t w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  for (uint32_t it = w0; it < n; it += nw) {
     const LargeItem item = F.items[it];
     const BigRec& R = F.recs[item.rec];
     const int y = (int)item.row + lane;
-    if (y > R.y1) continue;
-    const Setup S = rec_setup(R);
-    unsigned long long* row = F.vis + (size_t)y * F.v.W;
-    walk_row(S, persp, R.id, y, S.x0, S.x1,
-             [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
+    if (y <= R.y1) raster_rec_row(F, persp, R, y);
+  }
+  for (uint32_t it = w0; it < n_spill; it += nw) {
+    const LargeItem item = F.spill[it];
+    const BigRec& R = F.recs[item.rec];
+    for (int y = (int)item.row + lane; y <= R.y1; y += kLargeRows) raster_rec_row(F, persp, R, y);
   }
 }
 
@@ -1248,7 +1271,7 @@ static cudaError_t launch_coop(const void* fn, int grid, int block, void** args,
 // Launch sequence of one frame.  With F.g.va set, the vertex pass runs first
 // and the setup/resolve kernels read its buffers.  ev (optional, 6 events)
 // brackets the stages: clear+vertex, setup, large-triangle raster, -, resolve.
-cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev) {
+cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev, cudaEvent_t staged) {
   size_t npx = (size_t)F.v.W * F.v.H;
   const bool pre = F.g.va != nullptr;
   if (ev) cudaEventRecord(ev[0], st);
@@ -1256,7 +1279,9 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev)
   // kernel's atomics hit L2.
   int cgrid = grid_for(npx, 256);
   k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(
-      F.vis, npx, reinterpret_cast<uint32_t*>(F.counters), (uint32_t)(sizeof(Counters) / 4), nullptr, 0);
+      F.vis, npx, reinterpret_cast<uint32_t*>(F.counters), (uint32_t)(sizeof(Counters) / 4), nullptr, 0,
+      F.stage_src, F.stage_dst, F.stage_n16);
+  if (staged) cudaEventRecord(staged, st);  // the staging block has been read
   // vertex pass, setup and resolve may be scheduled while their predecessor
   // finishes (they wait for it before reading its output)
   cudaError_t le = cudaSuccess;
@@ -1310,7 +1335,7 @@ cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* 
   }
   if (B.small_max > 0 && B.n_px) {  // small triangles' visibility words of every scene
     int cgrid = grid_for(B.n_px, 256);
-    k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(B.vis, B.n_px, nullptr, 0, nullptr, 0);
+    k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(B.vis, B.n_px, nullptr, 0, nullptr, 0, nullptr, nullptr, 0);
   }
   if (ev) cudaEventRecord(ev[1], st);
   if (B.g.n_tris) {

@@ -90,12 +90,13 @@ struct Counters {
   unsigned int bin_overflow;
   unsigned int work_next;      // persistent-kernel work counter
   unsigned int item_count;     // large-triangle row blocks requested (single frames)
-  unsigned int item_overflow;
+  unsigned int spill_count;    // records whose remaining rows did not fit the row-block list
   unsigned int pad;
 };
 
 // One-frame launch.
-// Row block of a large sub-triangle: kLargeRows rows from `row` of record `rec`.
+// Row block of a large sub-triangle: kLargeRows rows from `row` of record
+// `rec`; in the spill list, every row from `row` to the record's last.
 struct LargeItem {
   uint32_t rec, row;
 };
@@ -110,6 +111,10 @@ struct FrameParams {
   uint32_t rec_cap;
   LargeItem* items;           // their row blocks
   uint32_t item_cap;
+  LargeItem* spill;           // rec_cap entries: records past the end of items[]
+  const uint4* stage_src;     // the frame's staging block in mapped pinned host memory,
+  uint4* stage_dst;           // fetched by the clear kernel (no copy-engine transfer)
+  uint32_t stage_n16;         // its size in 16-byte units
   uint8_t* rgb8;
   float* depth;
   float* rgbf;

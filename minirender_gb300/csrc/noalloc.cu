@@ -25,7 +25,7 @@
 
 namespace mrg {
 cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st);
-cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev);
+cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev, cudaEvent_t staged = nullptr);
 }  // namespace mrg
 
 using namespace mrg;
@@ -157,6 +157,7 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   F.rec_cap = 0;
   F.items = nullptr;
   F.item_cap = 0;
+  F.spill = nullptr;
   F.rgb8 = rgb8;
   F.depth = depth;
   F.ids = tri_id;

@@ -159,6 +159,30 @@ def big_triangles(w=300, h=200):
     return st, sc
 
 
+def tall_layers(w=8, h=16384, layers=800):
+    """Hundreds of layered triangles covering a tall frame: their 32-row
+    blocks outnumber the context's first row-block list, so the frame is
+    re-run with a larger one at the next synchronisation."""
+    rng = np.random.default_rng(4)
+    verts, tris = [], []
+    for k in range(layers):
+        z = -rng.uniform(30.0, 60.0)
+        base = len(verts)
+        dx = rng.uniform(-0.5, 0.5)
+        hw, top = rng.uniform(0.8, 3.0), rng.uniform(0.7, 6.0)
+        # tilted along y, and edges crossing the strip, so the nearest layer
+        # changes from row to row
+        verts += [[-hw + dx, -3, z], [dx, top, z + rng.uniform(-25, 25)], [hw + dx, -3, z]]
+        tris += [base, base + 2, base + 1]  # clockwise on screen: front-facing
+    nrm = rng.normal(size=(len(verts), 3)).astype(np.float32)
+    sc = Scene()
+    sc.add(TriMesh(np.array(verts, np.float32), nrm, np.array(tris, np.int32),
+                   material=Material(diffuse=(0.3, 0.7, 0.5), shininess=8)))
+    st = FrameState(width=w, height=h, projection=pj.projection_ortho(-1, 1, -1, 1, 1.0, 100.0),
+                    light=np.array([0.2, 0.4, 1], np.float32))
+    return st, sc
+
+
 ALL = {
     "ties": ties,
     "shared_edges": shared_edges,
