@@ -588,15 +588,34 @@ __device__ __forceinline__ void raster_small(const Setup (&S)[2], const int (&ki
   for (int s = 0; s < 2; s++)
     if (kind[s] == 1) span = max(span, max(S[s].x1 - S[s].x0, S[s].y1 - S[s].y0) + 1);
   if (__reduce_max_sync(0xffffffffu, (unsigned)span) <= 4u) {
+    // at most 4x4 pixels: the row and column loops have constant bounds and
+    // unroll, so the rows' independent edge evaluations interleave (each row
+    // still starts from its bounding-box edge and steps column by column)
 #pragma unroll
     for (int s = 0; s < 2; s++)
       if (kind[s] == 1) {
+        const Setup& Q = S[s];
         const uint32_t id = 2u * g + (uint32_t)s;
         const bool persp = T.perspective(tag);
-        for (int y = S[s].y0; y <= S[s].y1; y++) {
-          unsigned long long* row = T.row(tag, y);
-          walk_row(S[s], persp, id, y, S[s].x0, S[s].x1,
-                   [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
+#pragma unroll
+        for (int r = 0; r < 4; r++) {
+          const int y = Q.y0 + r;
+          if (y <= Q.y1) {
+            unsigned long long* row = T.row(tag, y);
+            float e1, e2;
+            row_start(Q, y, e1, e2);
+#pragma unroll
+            for (int c = 0; c < 4; c++) {
+              const int x = Q.x0 + c;
+              if (x <= Q.x1 && covered(e1, e2)) {
+                float k0, k1, k2;
+                const float z = frag_depth(Q, persp, e1, e2, k0, k1, k2);
+                if (z < 1e11f) atomicMin(row + x, ((unsigned long long)depth_key(z) << 32) | id);
+              }
+              e1 += Q.n1.x;
+              e2 += Q.n2.x;
+            }
+          }
         }
       }
     return;
