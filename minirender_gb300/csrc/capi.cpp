@@ -196,6 +196,7 @@ static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t 
   M.nidx = n_alias ? M.idx : (const int32_t*)take((size_t)4 * d->n_indices);
   M.tidx = t_alias ? M.idx : (const int32_t*)take((size_t)4 * (M.has_uv ? d->n_indices : 0));
   M.bad = (const uint32_t*)take((size_t)4 * ((M.n_tri + 31) / 32 + 1));
+  M.rec = mesh_wants_records(M.n_tri, M.n_pos) ? (const float4*)take(kRecBytes * (size_t)M.n_tri) : nullptr;
   if (d->n_vertices) CK(cudaMemcpyAsync((void*)M.pos, d->vertices, (size_t)12 * d->n_vertices, cudaMemcpyHostToDevice, st), "mesh copy");
   if (d->n_normals) CK(cudaMemcpyAsync((void*)M.nrm, d->normals, (size_t)12 * d->n_normals, cudaMemcpyHostToDevice, st), "mesh copy");
   if (M.has_uv) CK(cudaMemcpyAsync((void*)M.uv, d->texcoords, (size_t)8 * d->n_texcoords, cudaMemcpyHostToDevice, st), "mesh copy");
@@ -234,7 +235,8 @@ static size_t mesh_bytes(const mr_mesh_desc* d, bool has_uv) {
          align256((size_t)8 * (has_uv ? d->n_texcoords : 0)) + align256((size_t)4 * d->n_indices) +
          (n_alias ? 0 : align256((size_t)4 * d->n_indices)) +
          (t_alias ? 0 : align256((size_t)4 * (has_uv ? d->n_indices : 0))) +
-         align256((size_t)4 * ((ntri + 31) / 32 + 1));
+         align256((size_t)4 * ((ntri + 31) / 32 + 1)) +
+         (mesh_wants_records(ntri, d->n_vertices) ? align256(kRecBytes * (size_t)ntri) : 0);
 }
 
 int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes,

@@ -162,6 +162,25 @@ __device__ __forceinline__ void corners(const Geo& G, const DevRenderable& R, in
   }
 }
 
+// The view-space corners with attributes of triangle t from its corner
+// record: the same values corners<false, true> gathers (src/Renderer.cpp:
+// 344-348, 356-373).
+__device__ __forceinline__ void corners_rec(const DevRenderable& R, int t, Vtx (&v)[3]) {
+  const float4* r = R.mesh.rec + (size_t)8 * t;
+  float f[24];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    const float4 q = __ldg(r + k);
+    f[4 * k] = q.x; f[4 * k + 1] = q.y; f[4 * k + 2] = q.z; f[4 * k + 3] = q.w;
+  }
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    v[c].pos = affine(R.mv, v3(f[3 * c], f[3 * c + 1], f[3 * c + 2]));
+    v[c].nrm = affine(R.nm, v3(f[9 + 3 * c], f[9 + 3 * c + 1], f[9 + 3 * c + 2]));
+    v[c].uv = R.mesh.has_uv ? v2(f[18 + 2 * c], f[18 + 2 * c + 1]) : v2(0, 0);
+  }
+}
+
 struct Setup {
   V2 p0, p2, n1, n2;
   float z[3];
@@ -361,9 +380,13 @@ __device__ __forceinline__ const DevRenderable* winner_tri(const View& V, const 
   const int k = s_tb ? rs_lo + find_base(s_tb, 0, rs_hi - rs_lo, g) : find_base(G.tri_base, rs_lo, rs_hi, g);
   const DevRenderable* R = &G.rs[k];
   const int t = (int)(g - R->tri_base);
+  if (!PRE && R->mesh.rec) {
+    corners_rec(*R, t, vc);  // (ip is not used without the vertex pass)
+  } else {
 #pragma unroll
-  for (int c = 0; c < 3; c++) ip[c] = __ldg(R->mesh.idx + 3 * t + c);
-  corners<PRE, true>(G, *R, t, ip, vc);
+    for (int c = 0; c < 3; c++) ip[c] = __ldg(R->mesh.idx + 3 * t + c);
+    corners<PRE, true>(G, *R, t, ip, vc);
+  }
   const float zn = V.znear;
   clipped = vc[0].pos.z > zn || vc[1].pos.z > zn || vc[2].pos.z > zn;
   if (clipped) {
@@ -506,21 +529,42 @@ __global__ void k_clear(unsigned long long* vis, size_t n, uint32_t* z0, uint32_
   for (; i < n; i += stride) vis[i] = VIS_EMPTY;
 }
 
-__global__ void k_validate(DevMesh M, uint32_t* bad) {
+// Index check of a mesh upload (one bit per triangle), and for meshes with
+// corner records the gather of each valid triangle's corner attributes.
+__global__ void k_validate(DevMesh M, uint32_t* bad, float4* rec) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   bool b = false;
+  int ip[3] = {0, 0, 0}, in[3] = {0, 0, 0}, it[3] = {0, 0, 0};
   if (t < M.n_tri) {
     for (int c = 0; c < 3; c++) {
-      int ip = M.idx[3 * t + c], in = M.nidx[3 * t + c];
-      b |= ip < 0 || ip >= M.n_pos || in < 0 || in >= M.n_nrm;
+      ip[c] = M.idx[3 * t + c];
+      in[c] = M.nidx[3 * t + c];
+      b |= ip[c] < 0 || ip[c] >= M.n_pos || in[c] < 0 || in[c] >= M.n_nrm;
       if (M.has_uv) {
-        int it = M.tidx[3 * t + c];
-        b |= it < 0 || it >= M.n_uv;
+        it[c] = M.tidx[3 * t + c];
+        b |= it[c] < 0 || it[c] >= M.n_uv;
       }
     }
   }
   unsigned m = __ballot_sync(0xffffffffu, b);
   if ((threadIdx.x & 31) == 0 && (t >> 5) < ((M.n_tri + 31) >> 5)) bad[t >> 5] = m;
+  if (rec && t < M.n_tri && !b) {
+    float f[24];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      f[3 * c + 0] = M.pos[3 * ip[c] + 0];
+      f[3 * c + 1] = M.pos[3 * ip[c] + 1];
+      f[3 * c + 2] = M.pos[3 * ip[c] + 2];
+      f[9 + 3 * c + 0] = M.nrm[3 * in[c] + 0];
+      f[9 + 3 * c + 1] = M.nrm[3 * in[c] + 1];
+      f[9 + 3 * c + 2] = M.nrm[3 * in[c] + 2];
+      f[18 + 2 * c + 0] = M.has_uv ? M.uv[2 * it[c] + 0] : 0.f;
+      f[18 + 2 * c + 1] = M.has_uv ? M.uv[2 * it[c] + 1] : 0.f;
+    }
+    float4* r = rec + (size_t)8 * t;
+#pragma unroll
+    for (int k = 0; k < 6; k++) r[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+  }
 }
 
 // Vertex pass: threads [0, n_verts) transform and project positions,
@@ -1252,7 +1296,7 @@ static int sm_count() {
 
 cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st) {
   if (M.n_tri <= 0) return cudaSuccess;
-  k_validate<<<grid_for((size_t)M.n_tri, 256), 256, 0, st>>>(M, bad);
+  k_validate<<<grid_for((size_t)M.n_tri, 256), 256, 0, st>>>(M, bad, const_cast<float4*>(M.rec));
   return cudaGetLastError();
 }
 

@@ -58,7 +58,8 @@ struct Slot {
 size_t mesh_footprint(const mr_mesh_desc& d) {
   const size_t nt = (size_t)(d.n_indices / 3);
   return (size_t)12 * d.n_vertices + (size_t)12 * d.n_normals + (size_t)8 * d.n_texcoords +
-         (size_t)12 * d.n_indices + nt / 8 + 4096;
+         (size_t)12 * d.n_indices + nt / 8 + 4096 +
+         (mesh_wants_records((long long)nt, d.n_vertices) ? kRecBytes * nt : 0);
 }
 
 // Device bytes a request occupies while it runs: its outputs and the
