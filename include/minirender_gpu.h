@@ -246,7 +246,10 @@ MR_API int mr_set_batch_small_max(mr_ctx* ctx, int small_max);
  * count, sizes, renderable and triangle counts, tuning) into a CUDA graph and
  * replayed; cameras, lights and materials may change between replays. */
 MR_API int mr_set_batch_graphs(mr_ctx* ctx, int graphs);
-/* Queues the batch; outputs: MR_OUT_RGB8 | MR_OUT_DEPTH | MR_OUT_TRI_ID. */
+/* Queues the batch; outputs: MR_OUT_RGB8 | MR_OUT_DEPTH | MR_OUT_TRI_ID.
+ * A batch whose (tile, record) list overflowed is re-run when it is first
+ * waited for (mr_read_batch / mr_get_batch_stats), so the meshes and textures
+ * it reads must not be updated before then. */
 MR_API int mr_render_batch(mr_ctx* ctx, const mr_batch_scene* scenes, int32_t n_scenes,
                            const mr_renderable* renderables, int32_t n_renderables, int32_t outputs);
 /* Waits for the last batch and copies scene `scene`'s outputs to host memory. */

@@ -3,10 +3,12 @@
 //
 // Memory: the context owns every device buffer.  Meshes and textures are
 // allocated once at upload; frame buffers grow to the largest frame seen and
-// are then reused, so steady-state frames allocate nothing.  The one buffer
-// whose size is data dependent -- the (tile, triangle) bin list -- is
-// checked on the device; an overflow is detected at the next
-// synchronisation and the frame is re-run with a larger list.
+// are then reused, so steady-state frames allocate nothing.  The one
+// single-frame buffer whose size is data dependent -- the list of 32-row
+// blocks of large triangles -- is checked on the device: blocks past its end
+// go to a per-record spill list (which cannot overflow), and the list grows
+// for later frames.  Batches keep a (tile, record) list; an overflow there is
+// detected at the next synchronisation and the batch is re-run.
 #include "internal.h"
 
 extern "C" {
