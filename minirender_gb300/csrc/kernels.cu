@@ -977,15 +977,18 @@ __device__ __forceinline__ uint32_t block_scan(uint32_t v, uint32_t* s_part, uin
 // py0..py1): s_off[cn] is the number of (record, row) items.  Block-wide.
 __device__ __forceinline__ void stage_chunk(const BigRec* recs, const uint32_t* bins, uint32_t c0, uint32_t cn,
                                             int px0, int py0, int px1, int py1, BigRec* s_recs,
-                                            uint32_t* s_off) {
+                                            uint32_t* s_off, int* s_run = nullptr) {
   __syncthreads();  // the previous pass over s_recs / s_off is done
+  int run = 0;
   for (uint32_t i = threadIdx.x; i < cn; i += blockDim.x) {
     const BigRec r = recs[bins[c0 + i]];
     s_recs[i] = r;
     const int ys = max(r.y0, py0), ye = min(r.y1, py1);
     const bool hit = ys <= ye && max(r.x0, px0) <= min(r.x1, px1);
     s_off[i] = hit ? (uint32_t)(ye - ys + 1) : 0u;
+    if (hit) run = max(run, min(r.x1, px1) - r.x0);
   }
+  if (s_run && run) atomicMax(s_run, run);
   __syncthreads();
   if (threadIdx.x < 32) {  // one warp scans: each lane a contiguous run
     const int lane = (int)threadIdx.x;
@@ -1015,6 +1018,10 @@ __device__ __forceinline__ void stage_chunk(const BigRec* recs, const uint32_t* 
 // every record of the tile has been merged) stores, for each pixel, the
 // running edge values of the fragment that won it, so the resolve needs no
 // replay.  A pixel's winning word is unique (it holds the sub-triangle id).
+// Tiles whose records could make a pixel replay its winner's edge functions
+// over more columns than this capture the winners' edge values (pass 2).
+constexpr int kReplayMax = 256;
+
 template <bool CAPTURE>
 __device__ __forceinline__ void raster_items(const BigRec* s_recs, const uint32_t* s_off, uint32_t cn, int TW,
                                              int px0, int py0, int px1, int py1, bool persp,
@@ -1077,6 +1084,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
   __shared__ float s_dec[256];
   __shared__ uint32_t s_part[33];
   __shared__ uint32_t s_tile;
+  __shared__ int s_run;  // longest column replay a pixel of the tile could need
   __shared__ View s_view;
   __shared__ int s_meta[8];
   __shared__ uint32_t s_tb[kBatchTbMax];
@@ -1203,17 +1211,22 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
     const uint32_t s = (uint32_t)s_meta[6], e = (uint32_t)s_meta[7];
     const bool persp = s_view.persp != 0;
     const uint32_t nck = (e - s + (uint32_t)B.chunk - 1) / (uint32_t)B.chunk;
+    if (threadIdx.x == 0) s_run = 0;  // (ordered by stage_chunk's first barrier)
     for (uint32_t c = 0; c < nck; c++) {  // pass 1: depth test
       const uint32_t c0 = s + c * (uint32_t)B.chunk, cn = min((uint32_t)B.chunk, e - c0);
-      stage_chunk(B.recs, B.bins, c0, cn, px0, py0, px1, py1, s_recs, s_off);
+      stage_chunk(B.recs, B.bins, c0, cn, px0, py0, px1, py1, s_recs, s_off, &s_run);
       raster_items<false>(s_recs, s_off, cn, TW, px0, py0, px1, py1, persp, svis, s_e);
     }
-    for (uint32_t c = 0; c < nck; c++) {  // pass 2: the winners' edge values
-      const uint32_t c0 = s + c * (uint32_t)B.chunk, cn = min((uint32_t)B.chunk, e - c0);
-      if (nck > 1) stage_chunk(B.recs, B.bins, c0, cn, px0, py0, px1, py1, s_recs, s_off);
-      else __syncthreads();
-      raster_items<true>(s_recs, s_off, cn, TW, px0, py0, px1, py1, persp, svis, s_e);
-    }
+    // pass 2, the winners' edge values, only where a replay from the
+    // bounding-box edge could be long: otherwise the resolve replays (cheaper
+    // than walking every record of the tile a second time)
+    if (nck > 0 && s_run > kReplayMax)
+      for (uint32_t c = 0; c < nck; c++) {
+        const uint32_t c0 = s + c * (uint32_t)B.chunk, cn = min((uint32_t)B.chunk, e - c0);
+        if (nck > 1) stage_chunk(B.recs, B.bins, c0, cn, px0, py0, px1, py1, s_recs, s_off);
+        else __syncthreads();
+        raster_items<true>(s_recs, s_off, cn, TW, px0, py0, px1, py1, persp, svis, s_e);
+      }
     __syncthreads();
     for (int i = threadIdx.x; i < TP; i += nt) {
       const int x = px0 + i % TW, y = py0 + i / TW;
