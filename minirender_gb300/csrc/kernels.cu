@@ -1200,13 +1200,10 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
     const int lt = s_meta[1], tx = lt % s_meta[2], ty = lt / s_meta[2];
     const int px0 = tx * TW, py0 = ty * TH;
     const int px1 = min(px0 + TW, s_view.W) - 1, py1 = min(py0 + TH, s_view.H) - 1;
-    // the tile starts from the small triangles' words (or empty); captured
-    // edge values start as NaN (no fragment with a NaN edge value is ever
-    // written: its depth is NaN and fails z < 1e11f)
+    // the tile starts from the small triangles' words (or empty)
     for (int i = threadIdx.x; i < TP; i += nt) {
       const int x = px0 + i % TW, y = py0 + i / TW;
       svis[i] = (s_invis && x <= px1 && y <= py1) ? s_invis[(size_t)y * s_view.W + x] : VIS_EMPTY;
-      s_e[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
     }
     const uint32_t s = (uint32_t)s_meta[6], e = (uint32_t)s_meta[7];
     const bool persp = s_view.persp != 0;
@@ -1220,13 +1217,19 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
     // pass 2, the winners' edge values, only where a replay from the
     // bounding-box edge could be long: otherwise the resolve replays (cheaper
     // than walking every record of the tile a second time)
-    if (nck > 0 && s_run > kReplayMax)
+    const bool captured = nck > 0 && s_run > kReplayMax;
+    if (captured) {
+      // captured edge values start as NaN (no fragment with a NaN edge value
+      // is ever written: its depth is NaN and fails z < 1e11f); ordered
+      // before the capture by the barrier that opens each pass-2 chunk
+      for (int i = threadIdx.x; i < TP; i += nt) s_e[i] = make_float2(__int_as_float(0x7fc00000), 0.f);
       for (uint32_t c = 0; c < nck; c++) {
         const uint32_t c0 = s + c * (uint32_t)B.chunk, cn = min((uint32_t)B.chunk, e - c0);
         if (nck > 1) stage_chunk(B.recs, B.bins, c0, cn, px0, py0, px1, py1, s_recs, s_off);
         else __syncthreads();
         raster_items<true>(s_recs, s_off, cn, TW, px0, py0, px1, py1, persp, svis, s_e);
       }
+    }
     __syncthreads();
     for (int i = threadIdx.x; i < TP; i += nt) {
       const int x = px0 + i % TW, y = py0 + i / TW;
@@ -1246,7 +1249,7 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
                                                    tb_shared ? s_tb : nullptr);
         Setup S;
         float e1, e2;
-        const float2 ee = s_e[i];
+        const float2 ee = captured ? s_e[i] : make_float2(__int_as_float(0x7fc00000), 0.f);
         if (ee.x == ee.x) {  // won by a record of this tile: edge values captured
           winner_zterms<PRE>(s_view, B.g, R, ip, vc, clipped, S.z);
           e1 = ee.x;
