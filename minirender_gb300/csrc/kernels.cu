@@ -58,6 +58,13 @@ namespace mrg {
 // lets the successor's blocks start launching.
 __device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 __device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;"); }
+// 8-byte global-to-shared copy that bypasses registers (cp.async); the
+// thread's copies are complete after cp_async_wait_all().
+__device__ __forceinline__ void cp_async8(void* smem_dst, const void* gsrc) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(smem_dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 __device__ __forceinline__ int find_base(const uint32_t* base, int lo, int hi, uint32_t g) {
   while (hi - lo > 1) {
@@ -1200,11 +1207,15 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
     const int lt = s_meta[1], tx = lt % s_meta[2], ty = lt / s_meta[2];
     const int px0 = tx * TW, py0 = ty * TH;
     const int px1 = min(px0 + TW, s_view.W) - 1, py1 = min(py0 + TH, s_view.H) - 1;
-    // the tile starts from the small triangles' words (or empty)
+    // the tile starts from the small triangles' words (or empty), copied
+    // with cp.async so all of a thread's loads are in flight at once (made
+    // visible to the block by the barrier that opens pass 1)
     for (int i = threadIdx.x; i < TP; i += nt) {
       const int x = px0 + i % TW, y = py0 + i / TW;
-      svis[i] = (s_invis && x <= px1 && y <= py1) ? s_invis[(size_t)y * s_view.W + x] : VIS_EMPTY;
+      if (s_invis && x <= px1 && y <= py1) cp_async8(&svis[i], &s_invis[(size_t)y * s_view.W + x]);
+      else svis[i] = VIS_EMPTY;
     }
+    cp_async_wait_all();
     const uint32_t s = (uint32_t)s_meta[6], e = (uint32_t)s_meta[7];
     const bool persp = s_view.persp != 0;
     const uint32_t nck = (e - s + (uint32_t)B.chunk - 1) / (uint32_t)B.chunk;
