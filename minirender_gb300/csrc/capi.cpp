@@ -9,7 +9,31 @@
 // go to a per-record spill list (which cannot overflow), and the list grows
 // for later frames.  Batches keep a (tile, record) list; an overflow there is
 // detected at the next synchronisation and the batch is re-run.
+#include <thread>
+
 #include "internal.h"
+
+namespace {
+
+// Runs fn(begin, end) over [0, n) in contiguous ranges: on the calling thread
+// below `min_split` items, else on up to 8 host threads.
+template <class Fn>
+static void parallel_ranges(size_t n, size_t min_split, Fn fn) {
+  const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+  const size_t nt = std::min<size_t>({(size_t)8, hw, n / std::max<size_t>(min_split / 4, 1)});
+  if (n < min_split || nt <= 1) {
+    fn(0, n);
+    return;
+  }
+  std::vector<std::thread> pool;
+  const size_t per = (n + nt - 1) / nt;
+  for (size_t t = 1; t < nt; t++)
+    if (t * per < n) pool.emplace_back(fn, t * per, std::min(n, (t + 1) * per));
+  fn(0, std::min(n, per));
+  for (auto& th : pool) th.join();
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -941,6 +965,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   uint32_t* vbase = tb + (n_rs + 1);
   uint32_t* nbase = tb + 2 * (n_rs + 1);
   uint32_t* stb = tb + 3 * (n_rs + 1);
+  B.rs_scene.resize((size_t)n_rs);
   B.W.assign(n_scenes, 0);
   B.H.assign(n_scenes, 0);
   B.px_off.assign(n_scenes + 1, 0);
@@ -990,6 +1015,22 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
     SR.vis = B.small_max > 0 ? B.vis.p + B.px_off[s] : nullptr;
     for (int32_t i = sc[s].first_renderable; i < sc[s].first_renderable + sc[s].n_renderables; i++) {
       const MeshRec& m = c->meshes[rs[i].mesh];
+      B.rs_scene[i] = s;
+      tb[i] = tri;
+      vbase[i] = vb;
+      nbase[i] = nb;
+      tri += (uint32_t)m.d.n_tri;
+      vb += (uint32_t)m.d.n_pos;
+      nb += (uint32_t)m.d.n_nrm;
+    }
+  }
+  // per-renderable matrices and materials (Renderer::paintMesh,
+  // src/Renderer.cpp:336-338), split over host threads for large batches
+  parallel_ranges((size_t)n_rs, 2048, [&](size_t b, size_t e) {
+    for (size_t i = b; i < e; i++) {
+      const int32_t s = B.rs_scene[i];
+      const mr_frame* f = &sc[s].frame;
+      const MeshRec& m = c->meshes[rs[i].mesh];
       DevRenderable& R = B.h_rs[i];
       memset(&R, 0, sizeof(R));
       float mv[16], inv[16], nm[16];
@@ -999,16 +1040,10 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
       memcpy(R.mv, mv, sizeof(R.mv));
       memcpy(R.nm, nm, sizeof(R.nm));
       R.mesh = m.d;
-      R.tri_base = tri;
-      R.vert_base = vb;
-      R.nrm_base = nb;
+      R.tri_base = tb[i];
+      R.vert_base = vbase[i];
+      R.nrm_base = nbase[i];
       R.scene = (uint32_t)s;
-      tb[i] = tri;
-      vbase[i] = vb;
-      nbase[i] = nb;
-      tri += (uint32_t)m.d.n_tri;
-      vb += (uint32_t)m.d.n_pos;
-      nb += (uint32_t)m.d.n_nrm;
       const mr_material& M = rs[i].material;
       memcpy(R.diffuse, M.diffuse, sizeof(R.diffuse));
       memcpy(R.specular, M.specular, sizeof(R.specular));
@@ -1023,7 +1058,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
         else R.texf = (const float*)T.mem;
       }
     }
-  }
+  });
   tb[n_rs] = tri;
   vbase[n_rs] = vb;
   nbase[n_rs] = nb;

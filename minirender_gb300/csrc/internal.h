@@ -109,6 +109,7 @@ struct BatchSlot {
   int grid = 0;
   int n_scenes = 0, n_rs = 0;
   std::vector<int> W, H;
+  std::vector<int32_t> rs_scene;  // scene of each renderable (staging)
   std::vector<size_t> px_off;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
