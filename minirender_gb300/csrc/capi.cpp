@@ -9,28 +9,105 @@
 // go to a per-record spill list (which cannot overflow), and the list grows
 // for later frames.  Batches keep a (tile, record) list; an overflow there is
 // detected at the next synchronisation and the batch is re-run.
+#include <unistd.h>
+
+#include <condition_variable>
+#include <functional>
 #include <thread>
 
 #include "internal.h"
 
 namespace {
 
-// Runs fn(begin, end) over [0, n) in contiguous ranges: on the calling thread
-// below `min_split` items, else on up to 8 host threads.
+// Host worker threads for large staging loops, created on first use and
+// kept (spawning threads per batch cost more than the work they split).
+// One job at a time; the caller runs the first range itself.
+class HostPool {
+ public:
+  static HostPool& get() {
+    static HostPool pool;
+    return pool;
+  }
+  // Runs fn(begin, end) over [0, n) in up to size() + 1 contiguous ranges.
+  void run(size_t n, const std::function<void(size_t, size_t)>& fn) {
+    std::lock_guard<std::mutex> one(job_mu_);
+    // a forked child has none of the workers: it runs the job itself
+    const size_t parts = getpid() == pid_ ? std::min(n, workers_.size() + 1) : 1;
+    if (parts <= 1) {
+      fn(0, n);
+      return;
+    }
+    const size_t per = (n + parts - 1) / parts;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &fn;
+      n_ = n;
+      per_ = per;
+      parts_ = parts;
+      pending_ = parts - 1;
+      gen_++;
+    }
+    cv_.notify_all();
+    fn(0, std::min(n, per));
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [&] { return pending_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  HostPool() : pid_(getpid()) {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned nw = std::min(7u, hw > 1 ? hw - 1 : 0u);
+    for (unsigned t = 0; t < nw; t++) workers_.emplace_back([this, t] { loop(t + 1); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto& w : workers_) w.join();
+  }
+  void loop(size_t part) {
+    uint64_t seen = 0;
+    for (;;) {
+      const std::function<void(size_t, size_t)>* fn;
+      size_t b, e;
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+        if (part >= parts_) continue;  // fewer parts than workers this time
+        fn = fn_;
+        b = part * per_;
+        e = std::min(n_, b + per_);
+      }
+      if (b < e) (*fn)(b, e);
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  const pid_t pid_;
+  std::vector<std::thread> workers_;
+  std::mutex job_mu_, mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(size_t, size_t)>* fn_ = nullptr;
+  size_t n_ = 0, per_ = 0, parts_ = 0, pending_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// Runs fn(begin, end) over [0, n): on the calling thread below `min_split`
+// items, else split over the host pool.
 template <class Fn>
-static void parallel_ranges(size_t n, size_t min_split, Fn fn) {
-  const size_t hw = std::max(1u, std::thread::hardware_concurrency());
-  const size_t nt = std::min<size_t>({(size_t)8, hw, n / std::max<size_t>(min_split / 4, 1)});
-  if (n < min_split || nt <= 1) {
+void parallel_ranges(size_t n, size_t min_split, Fn fn) {
+  if (n < min_split) {
     fn(0, n);
     return;
   }
-  std::vector<std::thread> pool;
-  const size_t per = (n + nt - 1) / nt;
-  for (size_t t = 1; t < nt; t++)
-    if (t * per < n) pool.emplace_back(fn, t * per, std::min(n, (t + 1) * per));
-  fn(0, std::min(n, per));
-  for (auto& th : pool) th.join();
+  const std::function<void(size_t, size_t)> f = fn;
+  HostPool::get().run(n, f);
 }
 
 }  // namespace
