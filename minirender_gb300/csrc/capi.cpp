@@ -921,6 +921,15 @@ static int enqueue_batch(mr_ctx* c, BatchSlot& B, cudaStream_t st, cudaEvent_t* 
   CK(cudaMemcpyAsync(B.bases.p, B.h_u32, sizeof(uint32_t) * (3 * (n + 1) + S + 1), cudaMemcpyHostToDevice, st),
      "base upload");
   CK(cudaMemcpyAsync(B.scenes.p, B.h_scenes, sizeof(SceneRec) * S, cudaMemcpyHostToDevice, st), "scene upload");
+  // the host staging may be refilled once these copies are done (inside a
+  // graph capture this becomes an external event-record node, which the
+  // host can wait for after each launch of the graph)
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  CK(cudaStreamIsCapturing(st, &cap), "capture status");
+  if (cap == cudaStreamCaptureStatusActive)
+    CK(cudaEventRecordWithFlags(B.staged, st, cudaEventRecordExternal), "staging event");
+  else
+    CK(cudaEventRecord(B.staged, st), "staging event");
   CK(cudaMemsetAsync(B.d_cnt, 0, sizeof(Counters), st), "counter reset");
   CK(cudaMemsetAsync(B.tiles.p, 0, sizeof(uint32_t) * (3 * (size_t)B.P.n_tiles + 1), st), "tile reset");
   CK(launch_batch(B.P, B.threads, B.grid, B.block_sums.p, st, ev), "batch launch");
@@ -989,10 +998,11 @@ void BatchSlot::release() {
   if (exec) cudaGraphExecDestroy(exec);
   if (graph) cudaGraphDestroy(graph);
   if (done) cudaEventDestroy(done);
+  if (staged) cudaEventDestroy(staged);
   for (auto& e : ev)
     if (e) cudaEventDestroy(e);
   h_rs = nullptr; h_u32 = nullptr; h_scenes = nullptr; d_cnt = nullptr; h_cnt = nullptr;
-  exec = nullptr; graph = nullptr; done = nullptr;
+  exec = nullptr; graph = nullptr; done = nullptr; staged = nullptr;
   for (auto& e : ev) e = nullptr;
 }
 
@@ -1003,6 +1013,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   if (!B.d_cnt) CK(cudaMalloc(&B.d_cnt, sizeof(Counters)), "batch counters");
   if (!B.h_cnt) CK(cudaMallocHost(&B.h_cnt, sizeof(Counters)), "batch counters");
   if (!B.done) CK(cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming), "batch event");
+  if (!B.staged) CK(cudaEventCreateWithFlags(&B.staged, cudaEventDisableTiming), "batch event");
   uint64_t tris = 0, verts = 0, nrms = 0, pixels = 0, tiles = 0;
   const int TW = B.tile_w, TH = B.tile_h;
   for (int32_t s = 0; s < n_scenes; s++) {
@@ -1033,8 +1044,9 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
   if (tris >= ((uint64_t)1 << 31) || verts >= ((uint64_t)1 << 32) || nrms >= ((uint64_t)1 << 32) ||
       tiles >= ((uint64_t)1 << 31))
     return fail(c, MR_E_INVALID, "batch too large for 32-bit indices");
-  // staging (wait until the previous batch of this slot has consumed it)
-  CK(cudaEventSynchronize(B.done), "staging wait");
+  // staging (wait until the previous batch of this slot has copied it; its
+  // kernels may still run, so the host stages while the device renders)
+  CK(cudaEventSynchronize(B.staged), "staging wait");
   CK(pinned(B.h_rs, B.h_rs_cap, (size_t)n_rs), "pinned staging");
   CK(pinned(B.h_u32, B.h_u32_cap, (size_t)3 * (n_rs + 1) + n_scenes + 1), "pinned staging");
   CK(pinned(B.h_scenes, B.h_scenes_cap, (size_t)n_scenes), "pinned staging");

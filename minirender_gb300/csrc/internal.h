@@ -115,6 +115,7 @@ struct BatchSlot {
   cudaGraphExec_t exec = nullptr;
   std::vector<uint64_t> key;
   cudaEvent_t done = nullptr;
+  cudaEvent_t staged = nullptr;   // the batch's host staging has been copied
   bool have = false;
   cudaStream_t stream = nullptr;  // null: the context stream
   cudaEvent_t ev[8] = {};         // profiling events (slots other than the context's)
