@@ -277,9 +277,10 @@ MR_API int mr_set_profiling(mr_ctx* c, int on) {
 }
 
 // Copies the mesh arrays on st and checks the indices there, or -- when st
-// is the upload stream, which carries copies only so the next update never
-// waits for SMs -- on the compute stream once the next frame joins it.
-static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t st) {
+// is the upload stream (or the caller defers the check), which carries
+// copies only so the next transfer never waits for SMs -- later, before the
+// first launch that reads the mesh (join_upload, check_pending_meshes).
+static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t st, bool defer_check = false) {
   DevMesh& M = m.d;
   char* base = (char*)m.mem;
   size_t off = 0;
@@ -310,7 +311,7 @@ static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t 
     if (M.has_uv && !t_alias)
       CK(cudaMemcpyAsync((void*)M.tidx, d->texcoordsI, (size_t)4 * d->n_indices, cudaMemcpyHostToDevice, st), "mesh copy");
   }
-  if (c->upload && st == c->upload) m.validate_pending = true;
+  if (defer_check || (c->upload && st == c->upload)) m.validate_pending = true;
   else CK(launch_validate(M, (uint32_t*)M.bad, st), "validate launch");
   return MR_OK;
 }
@@ -343,7 +344,7 @@ static size_t mesh_bytes(const mr_mesh_desc* d, bool has_uv) {
 }
 
 int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes,
-                cudaMemPool_t pool) {
+                cudaMemPool_t pool, bool defer_check) {
   int rc = check_desc(c, d);
   if (rc) return rc;
   MeshRec m;
@@ -361,7 +362,7 @@ int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* 
     CK(pool ? cudaMallocFromPoolAsync(&m.mem, m.bytes, pool, stream) : cudaMallocAsync(&m.mem, m.bytes, stream),
        "mesh allocation");
   else CK(cudaMalloc(&m.mem, m.bytes), "mesh allocation");
-  rc = copy_mesh(c, m, d, st);
+  rc = copy_mesh(c, m, d, st, defer_check);
   if (rc) {
     if (stream) cudaFreeAsync(m.mem, stream);
     else cudaFree(m.mem);
@@ -378,6 +379,17 @@ int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* 
   }
   *out = h;
   if (bytes) *bytes = m.bytes;
+  return MR_OK;
+}
+
+int check_pending_mesh(mr_ctx* c, int32_t h, cudaStream_t st, bool* launched) {
+  if (launched) *launched = false;
+  if (h < 0 || h >= (int32_t)c->meshes.size() || !c->meshes[h].live) return fail(c, MR_E_HANDLE, "unknown mesh");
+  MeshRec& m = c->meshes[h];
+  if (!m.validate_pending) return MR_OK;
+  CK(launch_validate(m.d, (uint32_t*)m.d.bad, st), "validate launch");
+  m.validate_pending = false;
+  if (launched) *launched = true;
   return MR_OK;
 }
 

@@ -206,8 +206,13 @@ int batch_settle(mr_ctx* c, BatchSlot& B, cudaStream_t st);
 // Resident meshes/textures; with `stream` the memory is stream-ordered
 // (cudaMallocAsync / cudaFreeAsync) so no device-wide synchronisation occurs.
 // stream != null: stream-ordered allocation (from `pool` when given).
+// defer_check: the upload queues copies only; the index check runs at
+// check_pending_mesh (the server calls it right before the batch that first
+// reads the mesh, so its copies never wait behind kernels).
 int mesh_create(mr_ctx* c, const mr_mesh_desc* d, cudaStream_t stream, int32_t* out, size_t* bytes,
-                cudaMemPool_t pool = nullptr);
+                cudaMemPool_t pool = nullptr, bool defer_check = false);
+// Launches the deferred index check of mesh h on st (no-op if none pending).
+int check_pending_mesh(mr_ctx* c, int32_t h, cudaStream_t st, bool* launched);
 int mesh_destroy(mr_ctx* c, int32_t h, cudaStream_t stream);
 int texture_create(mr_ctx* c, const void* data, bool rgb8, int32_t rows, int32_t cols, cudaStream_t stream,
                    int32_t* out, cudaMemPool_t pool = nullptr);

@@ -158,8 +158,16 @@ void mr_server::launch(Slot* s, std::vector<Request*>& batch) {
           tready = textures[r->tex_key].ready;
         }
       }
-      // the upload may have run on another slot's stream
-      if (mready) cudaStreamWaitEvent(s->stream, mready, 0);
+      // a mesh uploaded for this batch: its deferred index check, then its
+      // ready event (other slots' batches wait on it); one uploaded for an
+      // earlier batch may have run on another slot's stream
+      bool checked = false;
+      if (check_pending_mesh(c, mh, s->stream, &checked) != MR_OK) rc = MR_E_CUDA;
+      if (checked) {
+        if (mready && cudaEventRecord(mready, s->stream) != cudaSuccess) rc = MR_E_CUDA;
+      } else if (mready) {
+        cudaStreamWaitEvent(s->stream, mready, 0);
+      }
       if (tready) cudaStreamWaitEvent(s->stream, tready, 0);
       scenes[i].frame = r->req.frame;
       scenes[i].first_renderable = (int32_t)i;
@@ -270,14 +278,21 @@ void mr_server::run() {
         queue.pop_front();
         committed += r->cost;
         // make the mesh / texture resident (upload is stream-ordered on this slot)
+        // (the uploads' CUDA calls run without the server lock, so submit and
+        // wait stay responsive; only this thread changes the resident maps)
         int rc = MR_OK;
         if (!meshes.count(r->mesh_key)) {
           Cached e;
-          std::lock_guard<std::recursive_mutex> g(c->mu);
-          rc = mesh_create(c, &r->req.mesh, s->stream, &e.handle, &e.bytes, pool);
-          if (rc == MR_OK && (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
-                              cudaEventRecord(e.ready, s->stream) != cudaSuccess))
-            rc = MR_E_CUDA;
+          lk.unlock();
+          {
+            std::lock_guard<std::recursive_mutex> g(c->mu);
+            // copies only: the index check runs right before this slot's
+            // batch (launch), which also records `ready`
+            rc = mesh_create(c, &r->req.mesh, s->stream, &e.handle, &e.bytes, pool, true);
+            if (rc == MR_OK && cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess)
+              rc = MR_E_CUDA;
+          }
+          lk.lock();
           if (rc == MR_OK) {
             meshes[r->mesh_key] = e;
             committed += e.bytes;
@@ -287,12 +302,16 @@ void mr_server::run() {
         if (rc == MR_OK && r->tex_key && !textures.count(r->tex_key)) {
           Cached e;
           e.bytes = (size_t)r->req.tex_rows * r->req.tex_cols * 3;
-          std::lock_guard<std::recursive_mutex> g(c->mu);
-          rc = texture_create(c, r->req.texture_rgb8, true, r->req.tex_rows, r->req.tex_cols, s->stream,
-                              &e.handle, pool);
-          if (rc == MR_OK && (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
-                              cudaEventRecord(e.ready, s->stream) != cudaSuccess))
-            rc = MR_E_CUDA;
+          lk.unlock();
+          {
+            std::lock_guard<std::recursive_mutex> g(c->mu);
+            rc = texture_create(c, r->req.texture_rgb8, true, r->req.tex_rows, r->req.tex_cols, s->stream,
+                                &e.handle, pool);
+            if (rc == MR_OK && (cudaEventCreateWithFlags(&e.ready, cudaEventDisableTiming) != cudaSuccess ||
+                                cudaEventRecord(e.ready, s->stream) != cudaSuccess))
+              rc = MR_E_CUDA;
+          }
+          lk.lock();
           if (rc == MR_OK) {
             textures[r->tex_key] = e;
             committed += e.bytes;
