@@ -161,8 +161,8 @@ def big_triangles(w=300, h=200):
 
 def tall_layers(w=8, h=16384, layers=800):
     """Hundreds of layered triangles covering a tall frame: their 32-row
-    blocks outnumber the context's first row-block list, so the frame is
-    re-run with a larger one at the next synchronisation."""
+    blocks outnumber the context's first row-block list, so most records are
+    rasterised through the spill list."""
     rng = np.random.default_rng(4)
     verts, tris = [], []
     for k in range(layers):

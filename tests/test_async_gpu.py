@@ -1,6 +1,7 @@
 """Asynchronous reads (mr_read_async + mr_wait): the same bytes as mr_read,
-two contexts with frames in flight at once, and the re-run of a frame whose
-large-triangle row-block list overflowed after its copies were queued."""
+two contexts with frames in flight at once, and a frame whose large-triangle
+row-block list overflowed (its remaining rows go through the spill list)
+read asynchronously and synchronously."""
 import numpy as np
 import pytest
 
@@ -92,9 +93,10 @@ def test_two_contexts_in_flight(product_lib):
 
 
 @pytest.mark.parametrize("mode", ["async", "sync"])
-def test_row_block_overflow_rerun(product_lib, mode):
-    """A fresh context's row-block list is too small for this frame; the
-    frame is re-run with a larger list before its outputs are handed over."""
+def test_row_block_overflow_spills(product_lib, mode):
+    """A fresh context's row-block list is too small for this frame: the
+    records whose blocks do not fit are rasterised from the spill list in the
+    same launch, so the frame is complete without a re-run."""
     from minirender_gb300.renderer import Renderer
     st, sc = E.tall_layers()
     ref = O.render(st, sc)
