@@ -45,7 +45,10 @@ UNIT = "frames/s"
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=30)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed steps (default: enough for several clock samples under load -- "
+                        "2000 frames for config1/config2, 200 for config3, 20 batches for config4; "
+                        "10 for --impl reference, whose steps are CPU frames on every host thread)")
     p.add_argument("--warmup", type=int, default=5)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="config2", choices=["config1", "config2", "config3", "config4", "config5"])
@@ -98,7 +101,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "100"],
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
@@ -819,8 +822,13 @@ def reference_arm(args, ws, rank):
     }
 
 
+DEFAULT_STEPS = {"config1": 2000, "config2": 2000, "config3": 200, "config4": 20, "config5": 1}
+
+
 def main():
     args = parse()
+    if args.steps is None:  # the reference arm's steps are whole CPU frames on every host thread
+        args.steps = DEFAULT_STEPS[args.workload] if args.impl == "gb300" else 10
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         out = reference_arm(args, ws, rank)
