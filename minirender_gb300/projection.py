@@ -5,7 +5,7 @@ projectionFrustum, projectionFrustumH, projectionCV) and the Matrix4
 constructors the samples use (translate, rotateX/Y/Z).  Every operation is a
 single numpy float32 scalar operation in the reference's order; tan/sin/cos
 are evaluated in double and rounded once.  These build *inputs*: the same
-matrix is handed to the device path and to the checker.
+matrix is handed to the device path and to the oracle.
 """
 from __future__ import annotations
 

@@ -4,12 +4,12 @@ edge cases the parity tests use.
 The primitive generators restate src/primitives.cpp (createCube :7-48,
 createCylinder :50-148, createSphere :150-230) with numpy; trigonometry is
 evaluated in double and rounded once to float32.  Everything here builds
-inputs only: the device path and the checker receive the same arrays.
+inputs only: the device path and the oracle receive the same arrays.
 
 Configs (sizes as stated in the benchmark definition):
   1  UV sphere 64 slices x 32 stacks, 640x480, point light, Blinn-Phong.
   2  icosphere level 8 (1,310,720 triangles) with value-noise displacement,
-     smooth normals, spherical UVs, 1024^2 RGB8 noise+checker texture,
+     smooth normals, spherical UVs, 1024^2 RGB8 noise+checkerboard texture,
      1920x1080, camera close enough that near-plane clipping runs.
   3  10M-triangle soup, 1-4 px^2 each, depth uniform in [0.2,50], 5% exact
      coplanar duplicates after their originals, per-face colour through a
@@ -265,7 +265,8 @@ def value_noise(p: np.ndarray, freq: float, seed: int) -> np.ndarray:
 
 
 def noise_texture(size: int, seed: int, checker: int = 8) -> np.ndarray:
-    """size x size RGB8: seeded uniform noise with a checker x checker overlay."""
+    """size x size RGB8: seeded uniform noise with a checker x checker
+    checkerboard overlay."""
     rng = np.random.default_rng(seed)
     noise = rng.integers(0, 256, (size, size, 3), dtype=np.int64)
     cell = max(1, size // checker)
