@@ -1,6 +1,6 @@
 // From-scratch stand-in for asl/String.h (see defs.h).  Restated semantics
 // (ASL's own implementation is not available, so these are choices, applied
-// identically to the checker and to the product's loaders):
+// identically to the oracle's reference build and to the product's loaders):
 //   split()            whitespace-separated tokens, empty tokens skipped
 //   split(c, out)      fields separated by c, empty fields kept
 //   (float)s / (int)s  strtod then cast to float / strtol base 10, 0 if not a number

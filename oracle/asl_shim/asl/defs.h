@@ -1,7 +1,7 @@
 // Minimal, from-scratch stand-in for the parts of the ASL library (aslze/asl
 // 1.11.14) that minirender's Renderer.cpp, Scene.cpp and primitives.cpp use.
 // ASL itself is not available here; this header restates the behaviour of its
-// public API only, so the reference sources compile unmodified as a checker.
+// public API only, so the reference sources compile unmodified into the oracle.
 // Test infrastructure: never linked into the product library.
 #ifndef ASL_SHIM_DEFS_H
 #define ASL_SHIM_DEFS_H

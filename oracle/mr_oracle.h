@@ -1,7 +1,7 @@
 /*
  * ORACLE -- test infrastructure only.  Nothing in the product library links,
  * loads or calls this code; tests, __graft_entry__.smoke() and the CPU
- * baseline of bench.py use it as the checker.
+ * baseline of bench.py use it as the oracle.
  *
  * Plain-C restatement of minirender's Renderer::render() hot path
  * (src/Renderer.cpp:13-20, 113-381 and src/Scene.cpp:13-36) with one

@@ -1,6 +1,6 @@
 """The library's model and image file loaders (host code, no GPU) against the
 reference's own loadMesh / loadSTL / loadOBJ / X3D reader / loadPPM /
-savePPM / saveSTL (src/io.cpp, src/x3d.cpp built as the checker): the same
+savePPM / saveSTL (src/io.cpp, src/x3d.cpp built into the oracle): the same
 scene tree, bit-identical arrays and materials, identical written files.
 Without the reference build the same models are checked against digests of
 the reference's output (tests/golden/loaders.json, tests/golden/make_golden.py)."""
