@@ -82,10 +82,18 @@ typedef struct mr_mesh_desc {
 /* One entry of Renderer::_renderables after Scene::collectShapes
  * (include/minirender/Scene.h:47-53, src/Scene.cpp:13-36): the mesh, its
  * world transform (row-major, m[4*i+j] = row i, column j) and the material
- * paintMesh would use (mesh->material, or the default, src/Renderer.cpp:336). */
+ * paintMesh would use (mesh->material, or the default, src/Renderer.cpp:336).
+ * flags (0 for scene renderables):
+ *   MR_RS_MODELVIEW  transform is the modelview itself: the frame's view is
+ *                    not applied (Renderer::paintTriangle's view-space
+ *                    vertices are a one-triangle mesh with the identity here)
+ *   MR_RS_NO_CLIP    no near-plane clipping (paintTriangle(..., world=false),
+ *                    src/Renderer.cpp:163-173) */
+#define MR_RS_MODELVIEW 1
+#define MR_RS_NO_CLIP   2
 typedef struct mr_renderable {
     int32_t mesh;
-    int32_t reserved;
+    int32_t flags;
     float transform[16];
     mr_material material;
 } mr_renderable;

@@ -21,6 +21,8 @@ MR_NOALLOC_MAX_SIDE = 4096
 MR_NOALLOC_MAX_PIXELS = 1 << 21
 MR_NOALLOC_MAX_TRIANGLES = 1 << 22
 MR_NO_TRIANGLE = 0xFFFFFFFF
+MR_RS_MODELVIEW = 1  # mr_renderable.flags: transform is the modelview
+MR_RS_NO_CLIP = 2    # mr_renderable.flags: no near-plane clipping
 
 MR_OUT_RGB8 = 1
 MR_OUT_DEPTH = 2
@@ -47,7 +49,7 @@ class mr_mesh_desc(C.Structure):
 
 
 class mr_renderable(C.Structure):
-    _fields_ = [("mesh", C.c_int32), ("reserved", C.c_int32), ("transform", F16),
+    _fields_ = [("mesh", C.c_int32), ("flags", C.c_int32), ("transform", F16),
                 ("material", mr_material)]
 
 

@@ -566,6 +566,7 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     int32_t t = rs[i].material.texture;
     if (t >= 0 && (t >= (int32_t)c->textures.size() || !c->textures[t].live))
       return fail(c, MR_E_HANDLE, "material refers to an unknown texture");
+    if (rs[i].flags & ~(MR_RS_MODELVIEW | MR_RS_NO_CLIP)) return fail(c, MR_E_INVALID, "unknown renderable flags");
     total += (uint64_t)c->meshes[h].d.n_tri;
   }
   if (total >= ((uint64_t)1 << 31)) return fail(c, MR_E_INVALID, "more than 2^31-1 triangles in one frame");
@@ -599,12 +600,14 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     const MeshRec& m = c->meshes[rs[i].mesh];
     DevRenderable& R = c->h_rs[i];
     float mv[16], inv[16], nm[16];
-    mat4_mul(f->view, rs[i].transform, mv);
+    if (rs[i].flags & MR_RS_MODELVIEW) memcpy(mv, rs[i].transform, sizeof(mv));
+    else mat4_mul(f->view, rs[i].transform, mv);
     mat4_inverse(mv, inv);
     mat4_transpose(inv, nm);
     memcpy(R.mv, mv, sizeof(R.mv));
     memcpy(R.nm, nm, sizeof(R.nm));
     R.mesh = m.d;
+    R.no_clip = (rs[i].flags & MR_RS_NO_CLIP) ? 1 : 0;
     R.tri_base = base;
     c->h_tri_base[i] = base;
     base += (uint32_t)m.d.n_tri;
@@ -1049,6 +1052,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
     int32_t t = rs[i].material.texture;
     if (t >= 0 && (t >= (int32_t)c->textures.size() || !c->textures[t].live))
       return fail(c, MR_E_HANDLE, "material refers to an unknown texture");
+    if (rs[i].flags & ~(MR_RS_MODELVIEW | MR_RS_NO_CLIP)) return fail(c, MR_E_INVALID, "unknown renderable flags");
     tris += (uint64_t)c->meshes[h].d.n_tri;
     verts += (uint64_t)c->meshes[h].d.n_pos;
     nrms += (uint64_t)c->meshes[h].d.n_nrm;
@@ -1135,12 +1139,14 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
       DevRenderable& R = B.h_rs[i];
       memset(&R, 0, sizeof(R));
       float mv[16], inv[16], nm[16];
-      mat4_mul(f->view, rs[i].transform, mv);
+      if (rs[i].flags & MR_RS_MODELVIEW) memcpy(mv, rs[i].transform, sizeof(mv));
+      else mat4_mul(f->view, rs[i].transform, mv);
       mat4_inverse(mv, inv);
       mat4_transpose(inv, nm);
       memcpy(R.mv, mv, sizeof(R.mv));
       memcpy(R.nm, nm, sizeof(R.nm));
       R.mesh = m.d;
+      R.no_clip = (rs[i].flags & MR_RS_NO_CLIP) ? 1 : 0;
       R.tri_base = tb[i];
       R.vert_base = vbase[i];
       R.nrm_base = nbase[i];

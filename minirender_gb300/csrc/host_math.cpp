@@ -154,7 +154,7 @@ MR_API int mr_collect_shapes(const mr_node* nodes, int32_t n_nodes, mr_renderabl
     if (nodes[i].mesh >= 0) {
       if (n < cap && out) {
         out[n].mesh = nodes[i].mesh;
-        out[n].reserved = 0;
+        out[n].flags = 0;
         memcpy(out[n].transform, &world[(size_t)16 * i], sizeof(float) * 16);
         out[n].material = nodes[i].has_material ? nodes[i].material : def;
       }

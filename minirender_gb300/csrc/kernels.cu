@@ -346,7 +346,9 @@ __device__ __forceinline__ bool setup_triangle(const View& V, const Geo& G, cons
   int ip[3];
 #pragma unroll
   for (int c = 0; c < 3; c++) ip[c] = __ldg(R.mesh.idx + 3 * t + c);
-  const float zn = V.znear;
+  // no_clip (paintTriangle(..., world=false)): never clipped, so the near
+  // test compares against +inf
+  const float zn = R.no_clip ? __int_as_float(0x7f800000) : V.znear;
   if (PRE) {
     float4 a[3];
 #pragma unroll
@@ -394,7 +396,7 @@ __device__ __forceinline__ const DevRenderable* winner_tri(const View& V, const 
     for (int c = 0; c < 3; c++) ip[c] = __ldg(R->mesh.idx + 3 * t + c);
     corners<PRE, true>(G, *R, t, ip, vc);
   }
-  const float zn = V.znear;
+  const float zn = R->no_clip ? __int_as_float(0x7f800000) : V.znear;
   clipped = vc[0].pos.z > zn || vc[1].pos.z > zn || vc[2].pos.z > zn;
   if (clipped) {
     Vtx sub[2][3];

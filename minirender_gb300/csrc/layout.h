@@ -49,6 +49,7 @@ struct DevRenderable {
   uint32_t nrm_base;    // global index of the first normal
   uint32_t scene;       // frame (scene) this renderable belongs to (batches)
   int32_t has_tex;      // texturing on and the material has a texture
+  int32_t no_clip;      // MR_RS_NO_CLIP: no near-plane clipping
   float diffuse[3], specular[3], emissive[3], shininess;
   const uint8_t* tex8;  // rows x cols x 3 bytes (decoded b/255), or
   const float* texf;    // rows x cols x 3 floats

@@ -173,7 +173,7 @@ void mr_server::launch(Slot* s, std::vector<Request*>& batch) {
       scenes[i].first_renderable = (int32_t)i;
       scenes[i].n_renderables = 1;
       rs[i].mesh = mh;
-      rs[i].reserved = 0;
+      rs[i].flags = 0;
       memcpy(rs[i].transform, r->req.transform, sizeof(rs[i].transform));
       rs[i].material = r->req.material;
       rs[i].material.texture = th;

@@ -5,8 +5,15 @@ Same method names and argument meaning as minirender::Renderer.  ``render``
 flattens the scene with Scene::collectShapes semantics, keeps meshes and
 textures resident on the device (re-uploaded only when a mesh's ``version``
 changes), and queues one frame through the C ABI; the getters read the
-results back.  The reference's paintMesh/paintTriangle are internal steps of
-``render`` here.
+results back.
+
+``paintMesh`` / ``paintTriangle`` draw into the current framebuffer as the
+reference's do: after ``clear()`` (or ``render()``) the paints are recorded
+and the next getter renders the scene's renderables and the paints, in call
+order, as one frame -- the same pixels as painting them one after the other
+(later fragments win only with a strictly smaller depth).  Frame-wide state
+(size, projection, light, lighting, texturing, background, normals) is the
+state when the frame is read.
 """
 from __future__ import annotations
 
@@ -29,6 +36,9 @@ class Renderer:
         self._textures: Dict[int, tuple] = {}   # id(array) -> (handle, array)
         self._out: Optional[dict] = None
         self._rendered = False
+        self._base = None                      # (renderables, count) of the last render()
+        self._paints: list = []                # paintMesh / paintTriangle since then
+        self._dirty = False
         self.outputs = abi.MR_OUT_DEFAULT | abi.MR_OUT_RGB_F32
 
     # ---- setters, include/minirender/Renderer.h:45-55
@@ -53,8 +63,8 @@ class Renderer:
         self.state.light_is_point = bool(point)
 
     def setMaterial(self, material: sc.Material):
-        # As in the reference, render() replaces the current material per mesh
-        # (src/Renderer.cpp:336), so this value is not used by render().
+        # As in the reference, render() and paintMesh replace the current
+        # material per mesh (src/Renderer.cpp:336); paintTriangle uses it.
         self._material = material
 
     def setLighting(self, on: bool):
@@ -74,6 +84,34 @@ class Renderer:
         depth 1e11f."""
         self._out = None
         self._rendered = False
+        self._base = None
+        self._paints = []
+        self._dirty = False
+
+    def paintMesh(self, mesh: sc.TriMesh, transform=None):
+        """Renderer::paintMesh (src/Renderer.cpp:334-381): the mesh with the
+        current view and `transform`, in the mesh's material (or the
+        default), over what is already drawn."""
+        mat = mesh.material if mesh.material is not None else sc.Material()
+        self._material = mat
+        xf = sc.identity() if transform is None else transform
+        self._paints.append(sc.Paint(mesh, xf, mat, 0))
+        self._dirty = True
+
+    def paintTriangle(self, a: sc.Vertex, b: sc.Vertex, c: sc.Vertex, world: bool = True):
+        """Renderer::paintTriangle (src/Renderer.cpp:163-309): one triangle
+        of view-space vertices in the current material; world=False skips the
+        near-plane clipping."""
+        mat = self._material if self._material is not None else sc.Material()
+        flags = abi.MR_RS_MODELVIEW | (0 if world else abi.MR_RS_NO_CLIP)
+        last = self._paints[-1] if self._paints else None
+        if last is not None and last.flags == flags and last.material is mat and getattr(last, "run", False):
+            sc.append_triangle(last, a, b, c)
+        else:
+            p = sc.triangle_paint(a, b, c, mat, world)
+            p.run = True
+            self._paints.append(p)
+        self._dirty = True
 
     # ---- frame
     def _mesh_handle(self, mesh: sc.TriMesh) -> int:
@@ -120,8 +158,28 @@ class Renderer:
         self.ctx.render(frame, rs, n, self.outputs)
         self._out = None
         self._rendered = True
+        self._base = (rs, n)
+        self._paints = []
+        self._dirty = False
+
+    def _flush_paints(self):
+        """Renders the last render()'s renderables and the paints since."""
+        base_rs, base_n = self._base if self._base is not None else (None, 0)
+        prs = sc.paints_to_c(self._paints, self._mesh_handle, self._texture_handle)
+        n = base_n + len(self._paints)
+        rs = (abi.mr_renderable * max(1, n))()
+        for i in range(base_n):
+            rs[i] = base_rs[i]
+        for j in range(len(self._paints)):
+            rs[base_n + j] = prs[j]
+        self.ctx.render(self.state.to_c(), rs, n, self.outputs)
+        self._rendered = True
+        self._dirty = False
+        self._out = None
 
     def _read(self) -> dict:
+        if self._dirty:
+            self._flush_paints()
         if self._out is None:
             if not self._rendered:
                 return self._cleared()

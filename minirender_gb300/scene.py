@@ -151,6 +151,65 @@ def flatten(scene: SceneNode) -> Flat:
     return Flat(nodes, meshes, textures)
 
 
+class Vertex:
+    """Vertex, include/minirender/Scene.h:14-24: position, normal, uv (the
+    arguments of Renderer::paintTriangle, in view space)."""
+
+    def __init__(self, position, normal=(0, 0, 1), uv=(0, 0)):
+        self.position = np.asarray(position, np.float32).reshape(3)
+        self.normal = np.asarray(normal, np.float32).reshape(3)
+        self.uv = np.asarray(uv, np.float32).reshape(2)
+
+
+class Paint:
+    """One paintMesh call (or a run of paintTriangle calls with one material
+    and one clipping mode, gathered into a mesh): the mesh, its transform
+    (the modelview itself when flags has MR_RS_MODELVIEW), the material and
+    the mr_renderable flags."""
+
+    def __init__(self, mesh: TriMesh, transform, material: Material, flags: int = 0):
+        self.mesh = mesh
+        self.transform = np.asarray(transform, np.float32).reshape(4, 4)
+        self.material = material
+        self.flags = int(flags)
+
+
+def triangle_paint(a: Vertex, b: Vertex, c: Vertex, material: Material, world: bool) -> Paint:
+    """paintTriangle(a, b, c, world) (src/Renderer.cpp:163-309) as a paint:
+    a one-triangle mesh of view-space vertices, the identity as modelview."""
+    v = [a, b, c]
+    idx = np.arange(3, dtype=np.int32)
+    mesh = TriMesh(np.stack([x.position for x in v]), np.stack([x.normal for x in v]), idx, normalsI=idx,
+                   texcoords=np.stack([x.uv for x in v]), texcoordsI=idx, material=material)
+    flags = abi.MR_RS_MODELVIEW | (0 if world else abi.MR_RS_NO_CLIP)
+    return Paint(mesh, identity(), material, flags)
+
+
+def append_triangle(p: Paint, a: Vertex, b: Vertex, c: Vertex) -> None:
+    """Adds one more triangle (drawn after the others) to a paintTriangle run."""
+    m = p.mesh
+    n = m.vertices.shape[0]
+    m.vertices = np.concatenate([m.vertices, np.stack([a.position, b.position, c.position])])
+    m.normals = np.concatenate([m.normals, np.stack([a.normal, b.normal, c.normal])])
+    m.texcoords = np.concatenate([m.texcoords, np.stack([a.uv, b.uv, c.uv])])
+    m.indices = np.concatenate([m.indices, np.arange(n, n + 3, dtype=np.int32)])
+    m.normalsI = m.indices
+    m.texcoordsI = m.indices
+
+
+def paints_to_c(paints: List[Paint], mesh_index, texture_index):
+    """mr_renderable array for a paint list; mesh_index(mesh) and
+    texture_index(texture) give the handles (or array indices)."""
+    rs = (abi.mr_renderable * max(1, len(paints)))()
+    for i, p in enumerate(paints):
+        rs[i].mesh = mesh_index(p.mesh)
+        rs[i].flags = p.flags
+        rs[i].transform[:] = [float(x) for x in p.transform.reshape(16)]
+        tex = p.material.texture
+        _fill_material(rs[i].material, p.material, texture_index(tex) if tex is not None else -1)
+    return rs
+
+
 def geometry_key(mesh: TriMesh) -> tuple:
     """Identity of a mesh's arrays: TriMesh nodes that share their arrays share
     one resident copy on the device."""

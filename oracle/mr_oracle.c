@@ -146,7 +146,7 @@ int mro_collect_shapes(const mr_node* nodes, int32_t n_nodes, mr_renderable* out
         if (nodes[i].mesh >= 0) {
             if (n < cap) {
                 out[n].mesh = nodes[i].mesh;
-                out[n].reserved = 0;
+                out[n].flags = 0;
                 memcpy(out[n].transform, world + 16 * i, sizeof(float) * 16);
                 out[n].material = nodes[i].has_material ? nodes[i].material : def;
             }
@@ -341,7 +341,10 @@ static int idx_ok(int32_t i, int32_t n) { return i >= 0 && i < n; }
 static void paint_mesh(Frame* F, const float* view, const mr_renderable* r, const mr_mesh_desc* m,
                        uint32_t tri_base) {
     float mv[16], inv[16], nm[16];
-    mro_mat4_mul(view, r->transform, mv); /* :337 */
+    if (r->flags & MR_RS_MODELVIEW) /* paintTriangle's view-space vertices (identity here) */
+        memcpy(mv, r->transform, sizeof(mv));
+    else
+        mro_mat4_mul(view, r->transform, mv); /* :337 */
     mro_mat4_inverse(mv, inv);           /* :338 */
     m4_transpose(inv, nm);
     V3* vv = (V3*)malloc(sizeof(V3) * (size_t)(m->n_vertices > 0 ? m->n_vertices : 1));
@@ -371,7 +374,8 @@ static void paint_mesh(Frame* F, const float* view, const mr_renderable* r, cons
             B.uv = v2(m->texcoords[2 * tb], m->texcoords[2 * tb + 1]);
             C.uv = v2(m->texcoords[2 * tc], m->texcoords[2 * tc + 1]);
         }
-        paint_triangle(F, &A, &B, &C, 1, 2u * (tri_base + (uint32_t)t));
+        /* world = false (no near-plane clipping) for MR_RS_NO_CLIP, :163-173 */
+        paint_triangle(F, &A, &B, &C, (r->flags & MR_RS_NO_CLIP) ? 0 : 1, 2u * (tri_base + (uint32_t)t));
     }
     free(vv);
     free(nn);

@@ -101,6 +101,9 @@ def ref_lib() -> Optional[C.CDLL]:
         L.ref_ppm_load.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.ref_ppm_save.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]
         L.ref_stl_save.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p]
+        L.ref_paint.restype = C.c_int
+        L.ref_paint.argtypes = [C.POINTER(abi.mr_frame), C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int,
+                                C.c_int32] + [C.c_void_p] * 8
         _ref = L
     return _ref
 
@@ -230,6 +233,61 @@ def render(state: FrameState, scene: sc.SceneNode, normals: bool = False) -> dic
     return out
 
 
+def render_paints(state: FrameState, paints, normals: bool = False, base_scene: sc.SceneNode = None) -> dict:
+    """The C restatement of clear(), then render()'s renderables of
+    `base_scene` (if given), then the paintMesh / paintTriangle calls
+    `paints` (scene.Paint) in order, as the reference paints them one after
+    the other (src/Renderer.cpp:163-381)."""
+    meshes, mesh_ix, texs, tex_ix = [], {}, [], {}
+
+    def mesh_index(m):
+        if id(m) not in mesh_ix:
+            mesh_ix[id(m)] = len(meshes)
+            meshes.append(m)
+        return mesh_ix[id(m)]
+
+    def texture_index(t):
+        if id(t) not in tex_ix:
+            tex_ix[id(t)] = len(texs)
+            texs.append(t)
+        return tex_ix[id(t)]
+
+    base = []
+    if base_scene is not None:
+        flat = sc.flatten(base_scene)
+        rs0, n0 = collect_shapes(flat)
+        for i in range(n0):
+            r = abi.mr_renderable()
+            C.memmove(C.addressof(r), C.addressof(rs0[i]), C.sizeof(r))
+            r.mesh = mesh_index(flat.meshes[rs0[i].mesh])
+            if r.material.texture >= 0:
+                r.material.texture = texture_index(flat.textures[r.material.texture])
+            base.append(r)
+    prs = sc.paints_to_c(list(paints), mesh_index, texture_index)
+    n = len(base) + len(paints)
+    rs = (abi.mr_renderable * max(1, n))()
+    for i, r in enumerate(base):
+        rs[i] = r
+    for j in range(len(paints)):
+        rs[len(base) + j] = prs[j]
+    descs = sc.mesh_descs(meshes)
+    tex, keep = _float_textures(texs)
+    f = state.to_c()
+    H, W = state.height, state.width
+    image = np.empty((H, W, 3), np.float32)
+    depth = np.empty((H, W), np.float32)
+    ids = np.empty((H, W), np.uint32)
+    nrm = np.empty((H, W, 3), np.float32) if normals else None
+    rc = lib().mro_render(C.byref(f), C.addressof(rs), n, C.addressof(descs), len(meshes), C.addressof(tex),
+                          len(texs), _ptr(image), _ptr(depth), _ptr(ids), _ptr(nrm) if nrm is not None else None)
+    if rc != 0:
+        raise RuntimeError(f"mro_render failed: {rc}")
+    out = {"image": image, "depth": depth, "ids": ids, "rgb8": quantize_rgb8(image)}
+    if nrm is not None:
+        out["normals"] = nrm
+    return out
+
+
 def range_image(state: FrameState, depth: np.ndarray) -> np.ndarray:
     f = state.to_c()
     depth = np.ascontiguousarray(depth, np.float32)
@@ -277,6 +335,56 @@ def ref_render(state: FrameState, scene: sc.SceneNode, normals: bool = False,
     if rng is not None:
         out["range"] = rng
     return out
+
+
+def ref_paint(state: FrameState, paints, clear: bool = False) -> dict:
+    """The reference Renderer itself: render() of an empty scene (the state
+    paintMesh uses), clear() if asked, then the paints in order -- paintMesh
+    for a scene.Paint without MR_RS_MODELVIEW, setMaterial + paintTriangle
+    per triangle of a paintTriangle run."""
+    L = ref_lib()
+    if L is None:
+        raise RuntimeError("reference build unavailable")
+    meshes, texs, tex_ix = [], [], {}
+    kind, mesh, xf, tri, world, mats = [], [], [], [], [], []
+
+    def texture_index(t):
+        if id(t) not in tex_ix:
+            tex_ix[id(t)] = len(texs)
+            texs.append(t)
+        return tex_ix[id(t)]
+
+    for p in paints:
+        m = abi.mr_material()
+        tex = p.material.texture
+        sc._fill_material(m, p.material, texture_index(tex) if tex is not None else -1)
+        if p.flags & abi.MR_RS_MODELVIEW:
+            v, n, uv = p.mesh.vertices, p.mesh.normals, p.mesh.texcoords
+            for t in range(p.mesh.indices.size // 3):
+                kind.append(1); mesh.append(-1); xf.append(np.eye(4, dtype=np.float32)); mats.append(m)
+                world.append(0 if p.flags & abi.MR_RS_NO_CLIP else 1)
+                tri.append(np.concatenate([np.concatenate([v[3 * t + c], n[3 * t + c], uv[3 * t + c]])
+                                           for c in range(3)]).astype(np.float32))
+        else:
+            kind.append(0); mesh.append(len(meshes)); meshes.append(p.mesh); xf.append(p.transform)
+            mats.append(m); world.append(1); tri.append(np.zeros(24, np.float32))
+    n = len(kind)
+    descs = sc.mesh_descs(meshes)
+    tex, keep = _float_textures(texs)
+    mat_arr = (abi.mr_material * max(1, n))(*mats)
+    kind_a = np.asarray(kind, np.int32); mesh_a = np.asarray(mesh, np.int32); world_a = np.asarray(world, np.int32)
+    xf_a = np.ascontiguousarray(np.stack(xf) if n else np.zeros((1, 4, 4)), np.float32)
+    tri_a = np.ascontiguousarray(np.stack(tri) if n else np.zeros((1, 24)), np.float32)
+    f = state.to_c()
+    H, W = state.height, state.width
+    image = np.empty((H, W, 3), np.float32)
+    depth = np.empty((H, W), np.float32)
+    rc = L.ref_paint(C.byref(f), C.addressof(descs), len(meshes), C.addressof(tex), len(texs), int(clear), n,
+                     _ptr(kind_a), _ptr(mesh_a), _ptr(xf_a), C.addressof(mat_arr), _ptr(tri_a), _ptr(world_a),
+                     _ptr(image), _ptr(depth))
+    if rc != 0:
+        raise RuntimeError(f"ref_paint failed: {rc}")
+    return {"image": image, "depth": depth, "rgb8": quantize_rgb8(image)}
 
 
 def ref_primitive(kind: int, a: float, b: float = 0.0, seg: int = 0, hseg: int = 0,

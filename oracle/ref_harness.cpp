@@ -303,4 +303,78 @@ void ref_stl_save(const char* path, const mr_mesh_desc* d, const float* transfor
   saveSTL(m, path);
 }
 
+// Material of a paint: diffuse/specular/emissive/shininess and a texture
+// index into tex (or -1).
+static Shared<Material> make_material(const mr_material& mm, const RefTexture* tex, int32_t n_tex) {
+  Shared<Material> mat = new Material();
+  mat->diffuse = Vec3(mm.diffuse[0], mm.diffuse[1], mm.diffuse[2]);
+  mat->specular = Vec3(mm.specular[0], mm.specular[1], mm.specular[2]);
+  mat->emissive = Vec3(mm.emissive[0], mm.emissive[1], mm.emissive[2]);
+  mat->shininess = mm.shininess;
+  if (mm.texture >= 0 && mm.texture < n_tex) {
+    const RefTexture& t = tex[mm.texture];
+    mat->texture.resize(t.rows, t.cols);
+    for (int a = 0; a < t.rows; a++)
+      for (int b = 0; b < t.cols; b++) {
+        const float* q = t.rgb + 3 * ((size_t)a * t.cols + b);
+        mat->texture(a, b) = Vec3(q[0], q[1], q[2]);
+      }
+  }
+  return mat;
+}
+
+// render() of an empty scene with the frame's state (which sets the light
+// direction, ambient and near plane paintMesh uses), optionally clear(),
+// then n_ops paints in order: kind 0 = paintMesh(meshes[mesh[i]] with
+// material[i], transform[16 i..]), kind 1 = setMaterial(material[i]) and
+// paintTriangle of tri[24 i..] (3 x position, normal, uv) with world[i].
+int ref_paint(const mr_frame* f, const mr_mesh_desc* meshes, int32_t n_meshes, const RefTexture* tex,
+              int32_t n_tex, int do_clear, int32_t n_ops, const int32_t* kind, const int32_t* mesh,
+              const float* transform, const mr_material* material, const float* tri, const int32_t* world,
+              float* image, float* depth) {
+  Shared<Scene> scene = new Scene();
+  scene->ambientLight = f->ambient;
+  Renderer r;
+  r.setBackground(Vec3(f->background[0], f->background[1], f->background[2]));
+  r.setSize(f->width, f->height);
+  r.setScene(scene);
+  r.setProjection(to_m4(f->projection));
+  r.setView(to_m4(f->view));
+  r.setLight(Vec3(f->light[0], f->light[1], f->light[2]), f->light_is_point != 0);
+  r.setLighting(f->lighting != 0);
+  r.setTexturing(f->texturing != 0);
+  r.render();
+  if (do_clear) r.clear();
+  std::vector<Shared<TriMesh>> keep;
+  for (int32_t i = 0; i < n_ops; i++) {
+    Shared<Material> mat = make_material(material[i], tex, n_tex);
+    if (kind[i] == 0) {
+      if (mesh[i] < 0 || mesh[i] >= n_meshes) return MR_E_HANDLE;
+      Shared<TriMesh> m = make_mesh(meshes[mesh[i]]);
+      m->material = mat;
+      keep.push_back(m);
+      r.paintMesh(m.ptr(), to_m4(transform + 16 * i));
+    } else {
+      r.setMaterial(mat);
+      const float* q = tri + 24 * i;
+      Vertex v[3];
+      for (int c = 0; c < 3; c++) {
+        const float* e = q + 8 * c;
+        v[c] = Vertex(Vec3(e[0], e[1], e[2]), Vec3(e[3], e[4], e[5]), Vec2(e[6], e[7]));
+      }
+      r.paintTriangle(v[0], v[1], v[2], world[i] != 0);
+    }
+  }
+  Array2<Vec3> img = r.getImage();
+  Array2<float> dep = r.getDepth();
+  size_t npx = (size_t)f->width * f->height;
+  for (size_t i = 0; i < npx; i++) {
+    image[3 * i] = img.data()[i].x;
+    image[3 * i + 1] = img.data()[i].y;
+    image[3 * i + 2] = img.data()[i].z;
+    depth[i] = dep.data()[i];
+  }
+  return MR_OK;
+}
+
 }  // extern "C"

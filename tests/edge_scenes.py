@@ -192,3 +192,42 @@ ALL = {
     "ortho_negative_z": ortho_negative_z,
     "big_triangles": big_triangles,
 }
+
+
+def paint_sequence(w=160, h=120):
+    """render() then paintMesh / paintTriangle calls (src/Renderer.cpp:
+    163-381): two meshes (one textured), a run of view-space triangles with
+    near-plane clipping (one crossing the near plane, one wholly behind it),
+    a run without clipping (world=false, one crossing), and the first mesh
+    painted again at the same place (exact ties: the earlier paint wins).
+    Returns (state, paints) as scene.Paint records."""
+    from minirender_gb300 import workloads as W
+    from minirender_gb300.scene import Paint, Vertex, append_triangle, triangle_paint
+    rng = np.random.default_rng(17)
+    _, s1 = W.config1(64, 48)
+    sphere = s1.children[0]
+    sphere.material = Material(diffuse=(0.8, 0.5, 0.3), shininess=32)
+    tex = rng.integers(0, 256, (16, 16, 3)).astype(np.uint8)
+    quad = _tri_mesh([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], [0, 1, 2, 0, 2, 3],
+                     uvs=[[0, 0], [2, 0], [2, 2], [0, 2]], material=Material(diffuse=(1, 1, 1), texture=tex))
+    st = FrameState(width=w, height=h, projection=_persp(w, h, near=0.5), view=pj.translate(0.2, -0.1, -4),
+                    light=np.array([2, 3, 4], np.float32), light_is_point=True)
+    t1 = pj.mat_mul(pj.translate(-0.6, 0, 0), pj.scale(0.8))
+    t2 = pj.mat_mul(pj.translate(0.7, 0.2, -0.5), pj.rotate_y(0.6))
+    paints = [Paint(sphere, t1, sphere.material), Paint(quad, t2, quad.material)]
+    m3 = Material(diffuse=(0.2, 0.9, 0.4), specular=(0.5, 0.5, 0.5), shininess=8, texture=tex)
+    # (vertex order clockwise on screen: front-facing)
+    tri = [Vertex((-1.5, -1.0, -3.0), (0, 0, 1), (0.1, 0.1)), Vertex((0.3, -0.8, -3.5), (0, 0.3, 1), (0.5, 0.8)),
+           Vertex((-0.5, 1.2, -2.5), (0.2, 0, 1), (0.9, 0.2))]
+    p = triangle_paint(*tri, m3, True)
+    append_triangle(p, Vertex((0.5, -0.5, -2.0), (0, 0, 1)), Vertex((1.5, -0.9, -2.2), (0, 0, 1)),
+                    Vertex((1.2, 0.6, -0.3), (0, 0, 1)))  # crosses the near plane (z = -0.5)
+    append_triangle(p, Vertex((0, 0, -0.2)), Vertex((0, 0.1, -0.1)), Vertex((0.1, 0, -0.3)))  # behind it
+    paints.append(p)
+    q = triangle_paint(Vertex((-1.2, 0.4, -2.8), (0, 0, 1), (0.3, 0.3)), Vertex((-0.9, -0.3, -3.1)),
+                       Vertex((-0.2, 0.9, -2.9)), m3, False)
+    # crosses the near plane, drawn unclipped
+    append_triangle(q, Vertex((-0.3, -0.3, -1.2)), Vertex((0.1, -0.35, -1.0)), Vertex((-0.1, -0.1, -0.45)))
+    paints.append(q)
+    paints.append(Paint(sphere, t1, Material(diffuse=(0.1, 0.1, 0.9))))
+    return st, paints

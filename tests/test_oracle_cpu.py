@@ -120,3 +120,16 @@ def test_oracle_matches_golden(oracle_lib, path):
 
 def test_golden_fixtures_present():
     assert len(glob.glob(os.path.join(GOLDEN, "*.npz"))) >= 8
+
+
+def test_paints_match_reference(ref_lib):
+    """paintMesh / paintTriangle sequences: the oracle's restatement is bit
+    for bit the reference's own Renderer, after render() and after clear()."""
+    import edge_scenes as E
+    st, paints = E.paint_sequence()
+    for clear in (False, True):
+        ref = O.ref_paint(st, paints, clear=clear)
+        got = O.render_paints(st, paints)
+        assert _bits_equal(got["depth"], ref["depth"]), clear
+        assert _bits_equal(got["image"], ref["image"]), clear
+        assert (got["ids"] != 0xFFFFFFFF).sum() > 1000

@@ -144,3 +144,63 @@ def test_empty_frames(renderer):
     sc = Scene()
     sc.add(TriMesh(np.zeros((0, 3), np.float32), np.zeros((0, 3), np.float32), np.zeros(0, np.int32)))
     _check("empty_mesh", st, sc, renderer)
+
+
+def _replay_paints(r, paints):
+    """The paint records as Renderer calls: paintMesh (a mesh sharing the
+    arrays but carrying the paint's material where they differ), and
+    setMaterial + paintTriangle per triangle of a triangle run."""
+    from minirender_gb300 import abi
+    from minirender_gb300.scene import TriMesh, Vertex
+    for p in paints:
+        if p.flags & abi.MR_RS_MODELVIEW:
+            r.setMaterial(p.material)
+            m = p.mesh
+            for t in range(m.indices.size // 3):
+                v = [Vertex(m.vertices[3 * t + c], m.normals[3 * t + c], m.texcoords[3 * t + c]) for c in range(3)]
+                r.paintTriangle(*v, world=not (p.flags & abi.MR_RS_NO_CLIP))
+        else:
+            mesh = p.mesh
+            if mesh.material is not p.material:
+                mesh = TriMesh(mesh.vertices, mesh.normals, mesh.indices, normalsI=mesh.normalsI,
+                               texcoords=mesh.texcoords, texcoordsI=mesh.texcoordsI, material=p.material)
+            r.paintMesh(mesh, p.transform)
+
+
+@pytest.mark.parametrize("clear", [False, True])
+def test_paint_mesh_and_triangles(renderer, clear):
+    """Renderer.paintMesh / paintTriangle after render() (and after clear()):
+    meshes, clipped and unclipped view-space triangles, exact ties -- the
+    same pixels as the oracle's paint sequence (pinned to the reference's
+    own paintMesh / paintTriangle)."""
+    from minirender_gb300.scene import Scene
+    st, paints = E.paint_sequence()
+    renderer.state = st
+    renderer.setScene(Scene())
+    renderer.render()
+    if clear:
+        renderer.clear()
+    _replay_paints(renderer, paints)
+    gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
+           "rgb8": renderer.getImageRGB8()}
+    stats = compare(gpu, O.render_paints(st, paints), f"paints_clear{int(clear)}")
+    _report(stats)
+    assert_parity(stats)
+    assert stats["covered"] > 5000
+
+
+def test_paint_over_rendered_scene(renderer):
+    """render() of a scene, then paintTriangle runs over it: the scene's
+    renderables come first in draw order."""
+    st, sc = W.config1(160, 120)
+    _, paints = E.paint_sequence(160, 120)
+    tri_runs = [p for p in paints if p.flags]
+    renderer.state = st
+    renderer.setScene(sc)
+    renderer.render()
+    _replay_paints(renderer, tri_runs)
+    gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
+           "rgb8": renderer.getImageRGB8()}
+    stats = compare(gpu, O.render_paints(st, tri_runs, base_scene=sc), "paints_over_scene")
+    _report(stats)
+    assert_parity(stats)
