@@ -45,10 +45,27 @@ def loader_digests():
     print("loaders.json:", ", ".join(sorted(out)))
 
 
+def paint_digests():
+    """tests/golden/paints.json: digests of the reference Renderer's image and
+    depth for the paintMesh / paintTriangle sequence of
+    tests/edge_scenes.paint_sequence, after render() and after clear()."""
+    import hashlib
+    import json
+    st, paints = E.paint_sequence()
+    out = {}
+    for clear in (False, True):
+        r = O.ref_paint(st, paints, clear=clear)
+        out[f"clear{int(clear)}"] = {k: hashlib.sha256(r[k].tobytes()).hexdigest() for k in ("image", "depth")}
+    with open(os.path.join(HERE, "paints.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("paints.json:", ", ".join(sorted(out)))
+
+
 def main():
     if O.ref_lib() is None:
         sys.exit("reference sources not available")
     loader_digests()
+    paint_digests()
     for name, (st, sc) in cases():
         r = O.ref_render(st, sc, normals=st.save_normals)
         expect = {"image": r["image"], "depth": r["depth"]}

@@ -133,3 +133,18 @@ def test_paints_match_reference(ref_lib):
         assert _bits_equal(got["depth"], ref["depth"]), clear
         assert _bits_equal(got["image"], ref["image"]), clear
         assert (got["ids"] != 0xFFFFFFFF).sum() > 1000
+
+
+def test_paints_match_golden():
+    """The oracle's paint sequence against the committed digests of the
+    reference's own paintMesh / paintTriangle (tests/golden/paints.json)."""
+    import hashlib
+    import json
+    import edge_scenes as E
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "paints.json")) as f:
+        want = json.load(f)
+    st, paints = E.paint_sequence()
+    for clear in (False, True):
+        got = O.render_paints(st, paints)
+        for k in ("image", "depth"):
+            assert hashlib.sha256(got[k].tobytes()).hexdigest() == want[f"clear{int(clear)}"][k], (clear, k)
