@@ -204,3 +204,18 @@ def test_paint_over_rendered_scene(renderer):
     stats = compare(gpu, O.render_paints(st, tri_runs, base_scene=sc), "paints_over_scene")
     _report(stats)
     assert_parity(stats)
+
+
+def test_unknown_renderable_flags_rejected(renderer):
+    from minirender_gb300 import capi
+    from minirender_gb300.scene import Scene
+    st, sc = W.config1(64, 48)
+    renderer.state = st
+    renderer.setScene(sc)
+    frame, rs, n = renderer.prepare()
+    rs[0].flags = 4
+    with pytest.raises(capi.MRError):
+        renderer.ctx.render(frame, rs, n, renderer.outputs)
+    rs[0].flags = 0
+    renderer.ctx.render(frame, rs, n, renderer.outputs)
+    renderer.setScene(Scene())
