@@ -38,6 +38,7 @@ struct Request {
   int result = MR_OK;
   int batch_size = 0;
   uint64_t mesh_key = 0, tex_key = 0;
+  bool mesh_ref = false, tex_ref = false;  // a reference taken by the upload-ahead stage
 };
 
 struct Cached {
@@ -93,6 +94,8 @@ struct mr_server {
   // to the budget mapped between uses (the default pool would return freed
   // memory to the system at every synchronisation and map it again).
   cudaMemPool_t pool = nullptr;
+  // uploads made ahead of a free slot for queued requests
+  cudaStream_t upload = nullptr;
   std::thread worker;
   bool stop = false;
   uint64_t next_ticket = 1;
@@ -102,6 +105,7 @@ struct mr_server {
   double t_first = 0, t_last = 0;
 
   void run();
+  void upload_ahead(std::unique_lock<std::mutex>& lk);
   bool evict_for(size_t need, Slot* s);
   void launch(Slot* s, std::vector<Request*>& batch);
   void retire(Slot* s);
@@ -161,13 +165,12 @@ void mr_server::launch(Slot* s, std::vector<Request*>& batch) {
       // a mesh uploaded for this batch: its deferred index check, then its
       // ready event (other slots' batches wait on it); one uploaded for an
       // earlier batch may have run on another slot's stream
+      // (a mesh uploaded ahead ran on the upload stream: wait for its copies
+      // before its check; waiting on a never-recorded event is a no-op)
+      if (mready) cudaStreamWaitEvent(s->stream, mready, 0);
       bool checked = false;
       if (check_pending_mesh(c, mh, s->stream, &checked) != MR_OK) rc = MR_E_CUDA;
-      if (checked) {
-        if (mready && cudaEventRecord(mready, s->stream) != cudaSuccess) rc = MR_E_CUDA;
-      } else if (mready) {
-        cudaStreamWaitEvent(s->stream, mready, 0);
-      }
+      if (checked && mready && cudaEventRecord(mready, s->stream) != cudaSuccess) rc = MR_E_CUDA;
       if (tready) cudaStreamWaitEvent(s->stream, tready, 0);
       scenes[i].frame = r->req.frame;
       scenes[i].first_renderable = (int32_t)i;
@@ -254,6 +257,65 @@ void mr_server::retire(Slot* s) {
   cv_done.notify_all();
 }
 
+// While every slot is busy: makes the meshes and textures of the next
+// queued requests (up to two batches ahead, in queue order) resident on the
+// upload stream, so the host link keeps working and a slot that frees finds
+// them there.  Each upload holds a reference for its request (no eviction
+// before use) and records `ready` after its copies; the index check runs
+// with the batch (launch).  Never evicts: it stops at the budget.  Called
+// with m held; releases it around the CUDA calls.
+void mr_server::upload_ahead(std::unique_lock<std::mutex>& lk) {
+  // by position: a submit may append while the lock is released (which
+  // would invalidate deque iterators); only this thread removes entries
+  for (size_t i = 0; i < queue.size() && i < (size_t)(2 * o.max_batch); i++) {
+    Request* r = queue[i];
+    const bool need_mesh = !r->mesh_ref && !meshes.count(r->mesh_key);
+    const bool need_tex = r->tex_key && !r->tex_ref && !textures.count(r->tex_key);
+    if (!need_mesh && !need_tex) continue;
+    const size_t tex_bytes = (size_t)r->req.tex_rows * r->req.tex_cols * 3;
+    const size_t extra = (need_mesh ? mesh_footprint(r->req.mesh) : 0) + (need_tex ? tex_bytes : 0);
+    if (committed + extra > o.budget_bytes) break;
+    Cached me, te;
+    int rc = MR_OK;
+    lk.unlock();
+    {
+      std::lock_guard<std::recursive_mutex> g(c->mu);
+      if (need_mesh) {
+        rc = mesh_create(c, &r->req.mesh, upload, &me.handle, &me.bytes, pool, true);
+        if (rc == MR_OK && (cudaEventCreateWithFlags(&me.ready, cudaEventDisableTiming) != cudaSuccess ||
+                            cudaEventRecord(me.ready, upload) != cudaSuccess))
+          rc = MR_E_CUDA;
+      }
+      if (rc == MR_OK && need_tex) {
+        te.bytes = tex_bytes;
+        rc = texture_create(c, r->req.texture_rgb8, true, r->req.tex_rows, r->req.tex_cols, upload, &te.handle,
+                            pool);
+        if (rc == MR_OK && (cudaEventCreateWithFlags(&te.ready, cudaEventDisableTiming) != cudaSuccess ||
+                            cudaEventRecord(te.ready, upload) != cudaSuccess))
+          rc = MR_E_CUDA;
+      }
+    }
+    lk.lock();
+    if (rc != MR_OK) break;  // the slot's own upload path reports the error
+    // (only this thread changes the maps and the queue's front, so
+    // position i still holds r)
+    if (need_mesh) {
+      me.refs = 1;
+      meshes[r->mesh_key] = me;
+      committed += me.bytes;
+      resident += me.bytes;
+      r->mesh_ref = true;
+    }
+    if (need_tex) {
+      te.refs = 1;
+      textures[r->tex_key] = te;
+      committed += te.bytes;
+      resident += te.bytes;
+      r->tex_ref = true;
+    }
+  }
+}
+
 void mr_server::run() {
   cudaSetDevice(c->device);
   std::unique_lock<std::mutex> lk(m);
@@ -320,6 +382,8 @@ void mr_server::run() {
         }
         if (rc != MR_OK) {
           committed -= r->cost;
+          if (r->mesh_ref && meshes.count(r->mesh_key)) meshes[r->mesh_key].refs--;
+          if (r->tex_ref && textures.count(r->tex_key)) textures[r->tex_key].refs--;
           r->result = rc;
           r->status = 0;
           r->t_done = now_us();
@@ -327,10 +391,11 @@ void mr_server::run() {
           cv_done.notify_all();
           continue;
         }
-        meshes[r->mesh_key].refs++;
+        // one reference per request (the upload-ahead stage may hold it already)
+        if (!r->mesh_ref) meshes[r->mesh_key].refs++;
         meshes[r->mesh_key].last_use = ++use_clock;
         if (r->tex_key) {
-          textures[r->tex_key].refs++;
+          if (!r->tex_ref) textures[r->tex_key].refs++;
           textures[r->tex_key].last_use = use_clock;
         }
         batch.push_back(r);
@@ -341,7 +406,10 @@ void mr_server::run() {
       lk.lock();
       launched = true;
     }
-    if (!launched) cv_work.wait_for(lk, std::chrono::microseconds(50));
+    if (!launched) {
+      upload_ahead(lk);
+      cv_work.wait_for(lk, std::chrono::microseconds(50));
+    }
   }
 }
 
@@ -391,6 +459,15 @@ MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out)
       return MR_E_CUDA;
     }
     s->slots.push_back(sl);
+  }
+  if (cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking) != cudaSuccess) {
+    for (Slot* x : s->slots) {
+      cudaStreamDestroy(x->stream);
+      delete x;
+    }
+    if (s->pool) cudaMemPoolDestroy(s->pool);
+    delete s;
+    return MR_E_CUDA;
   }
   s->worker = std::thread([s] { s->run(); });
   *out = s;
@@ -490,6 +567,7 @@ MR_API int mr_server_destroy(mr_server* s) {
   {
     std::lock_guard<std::recursive_mutex> g(s->c->mu);
     cudaSetDevice(s->c->device);
+    if (s->upload) cudaStreamSynchronize(s->upload);
     for (Slot* sl : s->slots) cudaStreamSynchronize(sl->stream);
     for (auto& kv : s->meshes) {
       mesh_destroy(s->c, kv.second.handle, s->slots[0]->stream);
@@ -505,6 +583,7 @@ MR_API int mr_server_destroy(mr_server* s) {
       cudaStreamDestroy(sl->stream);
       delete sl;
     }
+    if (s->upload) cudaStreamDestroy(s->upload);
     if (s->pool) cudaMemPoolDestroy(s->pool);  // every allocation from it has been freed
   }
   for (auto& kv : s->reqs) delete kv.second;
