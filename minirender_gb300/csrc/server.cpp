@@ -8,8 +8,12 @@
 // and textures that are not resident yet (stream-ordered allocation on the
 // slot's stream), stages the batch, launches it and queues the copies of each
 // request's outputs to its host buffers -- then returns to the queue while
-// the batch runs.  Finished slots are detected with non-blocking event
-// queries; their requests are marked done with their latency.
+// the batch runs.  A new mesh's copies are queued without a kernel between
+// them; its index check runs right before the batch that first reads it.
+// While every slot is busy, the meshes and textures of the next queued
+// requests are uploaded ahead on a stream of their own.  Finished slots are
+// detected with non-blocking event queries; their requests are marked done
+// with their latency.  The server lock is not held during CUDA calls.
 //
 // Meshes and textures stay resident in an LRU cache keyed by the caller's
 // ids; an entry no queued or running request refers to is evicted when the
