@@ -34,7 +34,7 @@ extern "C" {
 #define MR_API __attribute__((visibility("default")))
 #endif
 
-#define MR_ABI_VERSION 1
+#define MR_ABI_VERSION 2
 
 /* Status codes. */
 #define MR_OK 0
@@ -106,6 +106,8 @@ typedef struct mr_node {
     float transform[16];
     int32_t has_material;      /* 0: the Renderer's default material */
     mr_material material;
+    float opacity;             /* Material::opacity (OBJ "d", src/io.cpp:288-289;
+                                  1 by default); the renderer does not use it */
 } mr_node;
 
 /* Renderer state read by Renderer::render() (src/Renderer.cpp:311-332). */

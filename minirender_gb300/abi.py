@@ -55,7 +55,7 @@ class mr_renderable(C.Structure):
 
 class mr_node(C.Structure):
     _fields_ = [("parent", C.c_int32), ("mesh", C.c_int32), ("transform", F16),
-                ("has_material", C.c_int32), ("material", mr_material)]
+                ("has_material", C.c_int32), ("material", mr_material), ("opacity", C.c_float)]
 
 
 class mr_frame(C.Structure):

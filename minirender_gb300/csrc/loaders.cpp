@@ -245,7 +245,7 @@ struct mr_model {
   std::vector<Texture> textures;
   std::map<std::string, int32_t> texture_of_path;
 
-  int add_node(int parent, int mesh, const M4& xf, bool has_mat, const mr_material& mat) {
+  int add_node(int parent, int mesh, const M4& xf, bool has_mat, const mr_material& mat, float opacity = 1.0f) {
     mr_node n;
     memset(&n, 0, sizeof n);
     n.parent = parent;
@@ -253,6 +253,7 @@ struct mr_model {
     memcpy(n.transform, xf.m, sizeof n.transform);
     n.has_material = has_mat ? 1 : 0;
     n.material = has_mat ? mat : default_material();
+    n.opacity = has_mat ? opacity : 1.0f;
     nodes.push_back(n);
     return (int)nodes.size() - 1;
   }
@@ -477,6 +478,7 @@ void obj_parse_lines(const char* b, const char* e, ObjChunk& c) {
 // default material.
 struct ObjMaterial {
   mr_material m = default_material();
+  float opacity = 1.0f;
   std::string texture_name;
 };
 using MatPtr = std::shared_ptr<ObjMaterial>;
@@ -509,6 +511,8 @@ void obj_mtllib(const std::string& path, std::map<std::string, MatPtr>& mats) {
     } else if (k == "Ns") {
       mt.m.shininess = fat(parts, 1);
       if (mt.m.shininess < 0.0001f) mt.m.shininess = 10;
+    } else if (k == "d") {
+      mt.opacity = fat(parts, 1);
     } else if (k == "map_Kd") {
       mt.texture_name = parts.size() > 1 ? parts[1] : std::string();
     }
@@ -588,7 +592,7 @@ int load_obj(const std::string& path, mr_model& M) {
     auto t = tex_of_mat.find(g.material.get());
     mat.texture = t == tex_of_mat.end() ? -1 : t->second;
     M.meshes.push_back(std::move(m));
-    M.add_node(root, (int)M.meshes.size() - 1, identity(), true, mat);
+    M.add_node(root, (int)M.meshes.size() - 1, identity(), true, mat, g.material->opacity);
   }
   return MR_OK;
 }

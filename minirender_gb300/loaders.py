@@ -61,7 +61,7 @@ def load_mesh(path: str) -> SceneNode:
                 if nd.has_material:
                     m = nd.material
                     node.material = Material(diffuse=m.diffuse[:], specular=m.specular[:], emissive=m.emissive[:],
-                                             shininess=m.shininess,
+                                             shininess=m.shininess, opacity=nd.opacity,
                                              texture=textures[m.texture] if m.texture >= 0 else None)
             else:
                 node = SceneNode(xf)

@@ -133,6 +133,7 @@ def flatten(scene: SceneNode) -> Flat:
         nd.transform[:] = [float(x) for x in np.asarray(node.transform, np.float32).reshape(16)]
         nd.mesh = -1
         nd.has_material = 0
+        nd.opacity = 1.0
         if isinstance(node, TriMesh):
             if id(node) not in mesh_ix:
                 mesh_ix[id(node)] = len(meshes)
@@ -147,6 +148,7 @@ def flatten(scene: SceneNode) -> Flat:
                         textures.append(tex)
                     t = tex_ix[id(tex)]
                 nd.has_material = 1
+                nd.opacity = float(node.material.opacity)
                 _fill_material(nd.material, node.material, t)
     return Flat(nodes, meshes, textures)
 

@@ -196,6 +196,7 @@ static void flatten(RefModel& M, const Shared<SceneNode>& n, int parent) {
   nd.mesh = -1;
   from_m4(n->transform, nd.transform);
   nd.material.texture = -1;
+  nd.opacity = 1.0f;
   if (TriMesh* t = dynamic_cast<TriMesh*>(n.ptr())) {
     nd.mesh = (int32_t)M.meshes.size();
     M.meshes.push_back(t);
@@ -208,6 +209,7 @@ static void flatten(RefModel& M, const Shared<SceneNode>& n, int parent) {
       nd.material.emissive[0] = m.emissive.x; nd.material.emissive[1] = m.emissive.y;
       nd.material.emissive[2] = m.emissive.z;
       nd.material.shininess = m.shininess;
+      nd.opacity = m.opacity;
       if (m.texture.rows() > 0) {
         int id = -1;
         for (size_t k = 0; k < M.textures.size(); k++)

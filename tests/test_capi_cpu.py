@@ -62,7 +62,7 @@ def test_struct_layouts_match_ctypes(tmp_path):
 
 
 def test_abi_version_and_status(product_lib):
-    assert product_lib.mr_abi_version() == 1
+    assert product_lib.mr_abi_version() == 2
     assert product_lib.mr_status_string(abi.MR_E_BAD_INDEX) == b"mesh index out of range"
 
 

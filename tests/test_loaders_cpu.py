@@ -79,7 +79,7 @@ def canonical(model):
         out.append(np.array(nd.transform[:], np.float32).tobytes())
         if nd.has_material:
             m = nd.material
-            out.append(np.array(list(m.diffuse) + list(m.specular) + list(m.emissive) + [m.shininess],
+            out.append(np.array(list(m.diffuse) + list(m.specular) + list(m.emissive) + [m.shininess, nd.opacity],
                                 np.float32).tobytes())
             t = model["textures"][m.texture] if m.texture >= 0 else None
             out.append(b"notex" if t is None else struct.pack("<ii", *t.shape[:2]) + t.astype(np.float32).tobytes())
