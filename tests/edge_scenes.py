@@ -7,7 +7,7 @@ import numpy as np
 
 from minirender_gb300 import projection as pj
 from minirender_gb300.frame import FrameState
-from minirender_gb300.scene import Material, Scene, TriMesh
+from minirender_gb300.scene import Material, Scene, SceneNode, TriMesh
 
 f32 = np.float32
 
@@ -231,3 +231,117 @@ def paint_sequence(w=160, h=120):
     paints.append(q)
     paints.append(Paint(sphere, t1, Material(diffuse=(0.1, 0.1, 0.9))))
     return st, paints
+
+
+def random_scene(seed: int):
+    """Seeded random scene for fuzzing the whole path: 1-4 meshes of 10-250
+    triangles, each either a soup (every corner its own vertex) or indexed
+    into a small shared vertex pool (3T >= 2V), with separate normal and
+    texcoord index arrays; random windings (about half are culled), tiny,
+    medium and screen-sized triangles, some crossing the near plane; meshes
+    nested under transformed group nodes and under each other, one
+    instanced twice; perspective or orthographic camera with a rotated and
+    shifted view; materials with u8 or f32 textures of odd sizes and UVs up
+    to 4, or none; directional or point light; lighting, texturing and the
+    normals output switched at random; odd frame sizes."""
+    rng = np.random.default_rng(9000 + seed)
+    w = int(rng.integers(17, 180))
+    h = int(rng.integers(13, 140))
+    persp = rng.random() < 0.7
+    if persp:
+        near = float(rng.uniform(0.3, 1.5))
+        proj = _persp(w, h, near=near, far=float(rng.uniform(30, 200)), fov=float(rng.uniform(35, 100)))
+        zlo, zhi = -12.0, -0.1
+    else:
+        near = 0.5
+        proj = pj.projection_ortho(-4, 4, -3, 3, near, 50.0)
+        zlo, zhi = -45.0, -0.1
+
+    def place(n):
+        z = rng.uniform(zlo, zhi, n)
+        spread = np.abs(z) * 0.7 if persp else np.full(n, 3.5)
+        xy = rng.uniform(-1, 1, (n, 2)) * spread[:, None]
+        return np.column_stack([xy, z])
+
+    def make_mesh(n_tri):
+        size_class = rng.choice(3, n_tri, p=[0.6, 0.3, 0.1])
+        scale = np.array([0.02, 0.3, 3.0])[size_class]
+        if rng.random() < 0.5:  # soup
+            c = place(n_tri)
+            verts = (c[:, None, :] + rng.normal(size=(n_tri, 3, 3)) * scale[:, None, None] *
+                     np.array([1, 1, 0.6])).reshape(-1, 3)
+            idx = np.arange(3 * n_tri, dtype=np.int32).reshape(-1, 3)
+        else:  # indexed: 3T >= 2V
+            n_v = max(3, int(1.5 * n_tri) // 2 + 1)
+            verts = place(n_v)
+            idx = np.empty((n_tri, 3), np.int32)
+            for t in range(n_tri):
+                a = int(rng.integers(n_v))
+                # near neighbours in a sorted pool keep most triangles moderate
+                nb = np.clip(a + rng.integers(-6, 7, 2), 0, n_v - 1)
+                idx[t] = [a, nb[0], nb[1]]
+            order = np.argsort(verts[:, 0] + 7 * verts[:, 1])
+            verts = verts[order]
+        if rng.random() < 0.1 and n_tri > 2:
+            idx[1, 2] = idx[1, 0]  # a repeated corner: zero area
+        n_n = int(rng.integers(1, 2 * n_tri + 2))
+        normals = rng.normal(size=(n_n, 3)) * rng.uniform(0.2, 3.0)
+        normals[np.abs(normals).sum(1) < 1e-3] = (0, 0, 1)
+        nidx = rng.integers(0, n_n, (n_tri, 3)).astype(np.int32)
+        kw = {}
+        if rng.random() < 0.6:
+            n_uv = int(rng.integers(1, 3 * n_tri + 1))
+            kw = dict(texcoords=rng.uniform(0.01, 4.0, (n_uv, 2)).astype(np.float32),
+                      texcoordsI=rng.integers(0, n_uv, 3 * n_tri).astype(np.int32))
+        mat = None
+        if rng.random() < 0.85:
+            tex = None
+            if rng.random() < 0.6:
+                rows, cols = int(rng.integers(1, 40)), int(rng.integers(1, 40))
+                if rng.random() < 0.5:
+                    tex = rng.integers(0, 256, (rows, cols, 3)).astype(np.uint8)
+                else:
+                    tex = rng.uniform(0, 1, (rows, cols, 3)).astype(np.float32)
+            shin = 0.0 if rng.random() < 0.2 else float(rng.uniform(1, 64))
+            mat = Material(diffuse=rng.uniform(0, 1, 3), specular=rng.uniform(0, 1, 3),
+                           emissive=rng.uniform(0, 0.3, 3) * (rng.random() < 0.3), shininess=shin, texture=tex)
+        flip = rng.random(n_tri) < 0.5
+        idx[flip] = idx[flip][:, [0, 2, 1]]
+        nidx[flip] = nidx[flip][:, [0, 2, 1]]
+        if "texcoordsI" in kw:
+            ti = kw["texcoordsI"].reshape(-1, 3)
+            ti[flip] = ti[flip][:, [0, 2, 1]]
+        return TriMesh(np.asarray(verts, np.float32), np.asarray(normals, np.float32), idx.reshape(-1),
+                       normalsI=nidx.reshape(-1), material=mat, **kw)
+
+    def jitter():
+        t = pj.mat_mul(pj.translate(*rng.uniform(-0.3, 0.3, 3)), pj.rotate_z(float(rng.uniform(-0.5, 0.5))))
+        return pj.mat_mul(t, pj.scale(float(rng.uniform(0.8, 1.2))))
+
+    sc = Scene()
+    meshes = [make_mesh(int(rng.integers(10, 250))) for _ in range(int(rng.integers(1, 5)))]
+    for k, m in enumerate(meshes):
+        where = rng.integers(3)
+        m.transform = jitter()
+        if where == 0 or k == 0:
+            sc.add(m)
+        elif where == 1:
+            g = SceneNode(jitter())
+            sc.add(g)
+            g.add(m)
+        else:
+            meshes[0].add(m)  # a mesh under a mesh: both transforms apply
+    if len(meshes) > 1 and rng.random() < 0.5:  # the last mesh drawn again elsewhere
+        g = SceneNode(jitter())
+        sc.add(g)
+        g.add(meshes[-1] if not meshes[-1].children else meshes[0])
+    view = pj.mat_mul(pj.translate(*rng.uniform(-0.3, 0.3, 2), float(rng.uniform(-0.05, 0.05))),
+                      pj.rotate_z(float(rng.uniform(-np.pi, np.pi))))
+    point = rng.random() < 0.4
+    light = (rng.uniform(-3, 3, 3) if point else rng.normal(size=3)).astype(np.float32)
+    st = FrameState(width=w, height=h, projection=proj, view=view, light=light, light_is_point=point,
+                    ambient=float(rng.uniform(0, 0.3)), background=rng.uniform(0, 1, 3).astype(np.float32),
+                    lighting=rng.random() < 0.85, texturing=rng.random() < 0.8,
+                    save_normals=rng.random() < 0.3)
+    sc.ambientLight = np.float32(st.ambient)  # Renderer::render reads the scene's (src/Renderer.cpp:322)
+    return st, sc

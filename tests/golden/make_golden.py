@@ -27,6 +27,8 @@ def cases():
     yield "config4_s3_128x96", (st, sc)
     for name, fn in sorted(E.ALL.items()):
         yield "edge_" + name, fn(128, 96) if name == "big_triangles" else fn()
+    for seed in range(4):
+        yield f"random_s{seed}", E.random_scene(seed)
 
 
 def loader_digests():

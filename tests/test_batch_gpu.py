@@ -140,6 +140,18 @@ def test_batch_of_triangle_soups(batch):
         batch.ctx.set_batch_small_max(64)
 
 
+def test_batch_of_random_scenes(batch):
+    """48 seeded random scenes of uneven sizes and triangle counts in one
+    batch (soups and indexed meshes, clipping, both projections, textures),
+    with and without graph replay."""
+    items = [E.random_scene(s) for s in range(48)]
+    refs = [O.render(st, sc) for st, sc in items]
+    for graphs in (False, True):
+        batch.ctx.set_batch_graphs(graphs)
+        _check_all(batch, items, refs, f"random_g{int(graphs)}")
+    batch.ctx.set_batch_graphs(True)
+
+
 def test_batch_with_empty_scenes(batch):
     """Scenes without renderables or with empty meshes come out as background
     (and do not disturb the other scenes of the batch)."""

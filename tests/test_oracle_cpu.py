@@ -52,6 +52,15 @@ def test_config4_vs_reference(oracle_lib, ref_lib, seed):
     _vs_ref(st, sc)
 
 
+@pytest.mark.parametrize("seed", range(48))
+def test_random_scene_vs_reference(oracle_lib, ref_lib, seed):
+    """Seeded random scenes (tests/edge_scenes.random_scene): soups and
+    indexed meshes, nested and instanced nodes, clipping, both projections,
+    textures of odd sizes, every lighting switch, normals output."""
+    st, sc = E.random_scene(seed)
+    _vs_ref(st, sc, normals=st.save_normals)
+
+
 @pytest.mark.parametrize("name", sorted(E.ALL))
 def test_edge_vs_reference(oracle_lib, ref_lib, name):
     st, sc = E.ALL[name]()

@@ -57,6 +57,15 @@ def test_config3_scaled(renderer):
     _check("config3_1M_1080p", st, sc, renderer)
 
 
+@pytest.mark.parametrize("seed", range(48))
+def test_random_scene(renderer, seed):
+    """Seeded random scenes: soups (corner records) and indexed meshes
+    (per-vertex pass), nested and instanced nodes, near-plane clipping,
+    both projections, odd frame and texture sizes, every lighting switch."""
+    st, sc = E.random_scene(seed)
+    _check(f"random_{seed}", st, sc, renderer)
+
+
 @pytest.mark.parametrize("seed", [0, 1, 2, 3])
 def test_config4_scenes(renderer, seed):
     st, sc = W.config4_scene(seed)
