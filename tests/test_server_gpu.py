@@ -161,3 +161,59 @@ def test_server_empty_mesh_request(ctx):
         assert _same(out, ref)
     finally:
         srv.close()
+
+
+def _random_requests(n=48):
+    """First mesh of each seeded random scene (soup or indexed, clipped, both
+    projections, odd frame sizes), with its node transform and an RGB8
+    texture or none (requests carry RGB8 textures only)."""
+    import dataclasses
+
+    import edge_scenes as E
+    from minirender_gb300.scene import Material, TriMesh
+    out = []
+    for seed in range(n):
+        st, sc = E.random_scene(seed)
+        st = dataclasses.replace(st, save_normals=False)
+        m = sc.children[0]
+        mat = m.material
+        if mat is not None and mat.texture is not None and mat.texture.dtype != np.uint8:
+            mat = Material(mat.diffuse, mat.specular, mat.emissive, mat.shininess)
+        alone = TriMesh(m.vertices, m.normals, m.indices, normalsI=m.normalsI,
+                        texcoords=m.texcoords if m.texcoords.size else None,
+                        texcoordsI=m.texcoordsI if m.texcoordsI.size else None, material=mat,
+                        transform=m.transform)
+        out.append((st, alone))
+    return out
+
+
+def test_server_random_scenes(ctx):
+    """Seeded random requests submitted at once from two threads: each
+    result equals the oracle's render of that request alone."""
+    from minirender_gb300.server import RenderServer
+    reqs = _random_requests()
+    refs = [_oracle(st, m) for st, m in reqs]
+    srv = RenderServer(ctx, budget_bytes=2 << 30, slots=3, max_batch=16)
+    try:
+        results = {}
+        lock = threading.Lock()
+
+        def client(part):
+            for i in range(part, len(reqs), 2):
+                st, m = reqs[i]
+                out = _buffers(st)
+                t = srv.submit(st, m, mesh_key=5000 + i, transform=m.transform, texture_key=7000 + i, out=out)
+                with lock:
+                    results[t] = (i, out)
+
+        th = [threading.Thread(target=client, args=(k,)) for k in range(2)]
+        for x in th:
+            x.start()
+        for x in th:
+            x.join()
+        for t, (i, out) in results.items():
+            assert srv.wait(t).status == 0
+            assert _same(out, refs[i]), f"random request {i} differs from the oracle"
+        assert len(results) == len(reqs)
+    finally:
+        srv.close()
