@@ -149,3 +149,132 @@ def write_all(d):
                 '</Scene></X3D>\n')
     names.append("scene.x3d")
     return names
+
+
+def _num(rng, x):
+    """One float in a random textual form (all parse to nearby values)."""
+    k = int(rng.integers(5))
+    x = float(np.float32(x))
+    if k == 0:
+        return repr(x)
+    if k == 1:
+        return f"{x:.4f}"
+    if k == 2:
+        return f"{x:.6e}"
+    if k == 3:
+        return f"{x:g}"
+    return f"{x:+.9g}"
+
+
+def _sep(rng):
+    return [" ", " ", "  ", "\t", " \t "][int(rng.integers(5))]
+
+
+def random_obj(d, seed):
+    """A seeded random OBJ + MTL pair: random counts of v / vn / vt (some
+    files without normals or texcoords), polygons of 3-6 corners in every
+    face form (v, v/vt, v//vn, v/vt/vn, and rarely v/vt/ with an empty
+    field), usemtl switches among defined, undefined and not-yet-defined
+    materials with mtllib at a random place, comments, blank lines, o / g / s
+    lines, tabs and runs of spaces, CRLF or LF, numbers in several notations;
+    materials with Kd before any newmtl, Ns 0, opacity, present and missing
+    textures.  Returns the OBJ's file name."""
+    rng = np.random.default_rng(500 + seed)
+    stem = f"rand{seed}"
+    nl = "\r\n" if rng.random() < 0.3 else "\n"
+    rows, cols = int(rng.integers(1, 9)), int(rng.integers(1, 9))
+    _ppm(os.path.join(d, stem + ".ppm"), rng.integers(0, 256, (rows, cols, 3)), comment=rng.random() < 0.5)
+    nmat = int(rng.integers(0, 5))
+    mt = []
+    if rng.random() < 0.3:
+        mt.append("Kd" + "".join(_sep(rng) + _num(rng, v) for v in rng.uniform(0, 1, 3)))
+    for k in range(nmat):
+        mt.append(f"newmtl m{k}")
+        for key in ("Kd", "Ks", "Ke"):
+            if rng.random() < 0.7:
+                mt.append(key + "".join(_sep(rng) + _num(rng, v) for v in rng.uniform(0, 1, 3)))
+        if rng.random() < 0.6:
+            mt.append("Ns" + _sep(rng) + ("0" if rng.random() < 0.25 else _num(rng, rng.uniform(1, 100))))
+        if rng.random() < 0.3:
+            mt.append("d " + _num(rng, rng.uniform(0, 1)))
+        if rng.random() < 0.4:
+            mt.append("map_Kd " + (stem + ".ppm" if rng.random() < 0.7 else "absent.ppm"))
+        if rng.random() < 0.3:
+            mt.append("")
+    with open(os.path.join(d, stem + ".mtl"), "w", newline="") as f:
+        f.write(nl.join(mt) + nl)
+
+    nv = int(rng.integers(3, 80))
+    has_vn, has_vt = rng.random() < 0.7, rng.random() < 0.6
+    nn = int(rng.integers(1, 60)) if has_vn else 0
+    nt = int(rng.integers(1, 60)) if has_vt else 0
+    decl = ["v"] * nv + ["vn"] * nn + ["vt"] * nt
+    rng.shuffle(decl)
+    lines = ["# random OBJ"]
+    for kind in decl:
+        if kind == "v":
+            vals = rng.uniform(-3, 3, 3)
+        elif kind == "vn":
+            vals = rng.normal(size=3)
+        else:
+            vals = rng.uniform(-0.5, 2, 2 + int(rng.random() < 0.2))
+        lines.append(kind + "".join(_sep(rng) + _num(rng, v) for v in vals) + (" " if rng.random() < 0.1 else ""))
+        if rng.random() < 0.03:
+            lines.append("")
+    names = [f"m{k}" for k in range(nmat)] + ["undefined"]
+    mtllib_at = int(rng.integers(-1, 20))  # face count before the mtllib line (-1: none)
+    forms = ["v"] + (["v/vt"] if has_vt else []) + (["v//vn"] if has_vn else []) + \
+            (["v/vt/vn"] if has_vt and has_vn else [])
+    n_faces = int(rng.integers(1, 60))
+    for k in range(n_faces):
+        if k == mtllib_at:
+            lines.append(f"mtllib {stem}.mtl")
+        r = rng.random()
+        if r < 0.15:
+            lines.append("usemtl " + names[int(rng.integers(len(names)))])
+        elif r < 0.18:
+            lines.append(["o part", "g group one", "s off", "s 1"][int(rng.integers(4))])
+        elif r < 0.2:
+            lines.append("# comment f 1 2 3")
+        m = int(rng.integers(3, 7))
+        ids = rng.choice(nv, min(m, nv), replace=False) + 1
+        form = forms[int(rng.integers(len(forms)))]
+        toks = []
+        for i in ids:
+            ti = int(rng.integers(1, nt + 1)) if nt else 0
+            ni = int(rng.integers(1, nn + 1)) if nn else 0
+            toks.append({"v": f"{i}", "v/vt": f"{i}/{ti}", "v//vn": f"{i}//{ni}",
+                         "v/vt/vn": f"{i}/{ti}/{ni}"}[form])
+        if has_vt and rng.random() < 0.03:
+            toks[0] = f"{ids[0]}/{max(1, nt)}/"
+        lines.append("f" + "".join(_sep(rng) + t for t in toks))
+    if mtllib_at >= n_faces:
+        lines.append(f"mtllib {stem}.mtl")
+    with open(os.path.join(d, stem + ".obj"), "w", newline="") as f:
+        f.write(nl.join(lines) + (nl if rng.random() < 0.8 else ""))
+    return stem + ".obj"
+
+
+def random_ascii_stl(d, seed):
+    """A seeded random ASCII STL: facets of 2-4 vertices (only 3-vertex
+    facets become triangles, the others' vertices still count), numbers in
+    several notations, tabs and runs of spaces, CRLF or LF, with or without
+    a solid name and the closing endsolid.  Returns the file name."""
+    rng = np.random.default_rng(700 + seed)
+    nl = "\r\n" if rng.random() < 0.4 else "\n"
+    lines = ["solid" + (" part_" + str(seed) if rng.random() < 0.7 else "")]
+    for k in range(int(rng.integers(1, 60))):
+        n = rng.normal(size=3)
+        lines.append(_sep(rng) + "facet" + _sep(rng) + "normal" + "".join(_sep(rng) + _num(rng, v) for v in n))
+        lines.append(_sep(rng) + "outer loop")
+        nvert = 3 if rng.random() < 0.9 else int(rng.choice([2, 4]))
+        for p in rng.uniform(-5, 5, (nvert, 3)):
+            lines.append(_sep(rng) + "vertex" + "".join(_sep(rng) + _num(rng, v) for v in p))
+        lines.append(_sep(rng) + "endloop")
+        lines.append(_sep(rng) + "endfacet")
+    if rng.random() < 0.8:
+        lines.append("endsolid")
+    name = f"rand{seed}.stl"
+    with open(os.path.join(d, name), "w", newline="") as f:
+        f.write(nl.join(lines) + nl)
+    return name

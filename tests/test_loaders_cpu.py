@@ -204,3 +204,26 @@ def test_errors(tmp_path, product_lib):
     assert node.children == []
     with pytest.raises(capi.MRError):
         loaders.load_ppm(str(bad))
+
+
+@pytest.mark.parametrize("seed", range(32))
+def test_random_obj_matches_reference(tmp_path, product_lib, ref_lib, seed):
+    """Seeded random OBJ + MTL files (tests/loader_files.random_obj): the
+    same scene tree, arrays and materials as the reference's loadOBJ."""
+    name = loader_files.random_obj(str(tmp_path), seed)
+    p = str(tmp_path / name)
+    ref = O.ref_load_mesh(p)
+    got = product_model(p)
+    assert ref is not None and got is not None
+    assert canonical(got) == canonical(ref)
+
+
+@pytest.mark.parametrize("seed", range(16))
+def test_random_ascii_stl_matches_reference(tmp_path, product_lib, ref_lib, seed):
+    """Seeded random ASCII STL files: the same mesh as the reference's loadSTLa."""
+    name = loader_files.random_ascii_stl(str(tmp_path), seed)
+    p = str(tmp_path / name)
+    ref = O.ref_load_mesh(p)
+    got = product_model(p)
+    assert ref is not None and got is not None
+    assert canonical(got) == canonical(ref)

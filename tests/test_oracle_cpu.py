@@ -67,8 +67,17 @@ def test_edge_vs_reference(oracle_lib, ref_lib, name):
     _vs_ref(st, sc, normals=st.save_normals)
 
 
-def test_range_image_vs_reference(oracle_lib, ref_lib):
-    st, sc = W.config1(160, 120)
+def _range_cases():
+    yield "config1", W.config1(160, 120)
+    for seed in range(0, 48, 4):
+        yield f"random{seed}", E.random_scene(seed)
+
+
+@pytest.mark.parametrize("case", list(_range_cases()), ids=lambda c: c[0])
+def test_range_image_vs_reference(oracle_lib, ref_lib, case):
+    """Renderer::getRangeImage (depth unprojected to view space), perspective
+    and orthographic: the restatement equals the reference build's."""
+    st, sc = case[1]
     o = O.render(st, sc)
     r = O.ref_render(st, sc, range_xyz=True)
     assert _bits_equal(O.range_image(st, o["depth"]), r["range"])
