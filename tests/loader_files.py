@@ -2,7 +2,8 @@
 material libraries, polygons and every face-index form, OBJ without normals,
 X3D with transforms, DEF/USE, both face-set kinds and an Inline, and PPM
 images with header comments.  write_all(dir) writes them and returns the
-list of model paths (relative names)."""
+list of model paths (relative names); random_obj, random_ascii_stl and
+random_x3d write one seeded random file each for the loader fuzz tests."""
 import os
 import struct
 
@@ -277,4 +278,122 @@ def random_ascii_stl(d, seed):
     name = f"rand{seed}.stl"
     with open(os.path.join(d, name), "w", newline="") as f:
         f.write(nl.join(lines) + nl)
+    return name
+
+
+def random_x3d(d, seed):
+    """A seeded random X3D scene: Transform / Group nodes nested up to three
+    deep with random translation, rotation and scale (or none); Shapes with
+    or without Appearance, Material (random subset of attributes, DEF and
+    USE), ImageTexture (present and missing files); IndexedFaceSet polygons
+    of 3-5 corners with and without normalIndex / texCoordIndex and a
+    trailing -1, or IndexedTriangleSet; Coordinate DEF / USE; number lists
+    separated by spaces, commas or both; both attribute quote styles.
+    Returns the file name."""
+    rng = np.random.default_rng(900 + seed)
+    _ppm(os.path.join(d, f"xrand{seed}.ppm"), rng.integers(0, 256, (int(rng.integers(1, 6)), int(rng.integers(1, 6)), 3)))
+    coord_defs = {}  # DEF name -> point count
+    mat_defs = []
+
+    def q(v):
+        return f"'{v}'" if rng.random() < 0.3 else f'"{v}"'
+
+    def nums(vals, ints=False, spaced=False):
+        # Transform fields and index lists are split at whitespace only (a
+        # bare comma would merge fields, and the reference reads past the end
+        # of a short list); point and vector lists also split at commas
+        seps = [" ", ", ", "  "] if spaced or ints else [" ", ", ", ",", "  "]
+        sep = seps[int(rng.integers(len(seps)))]
+        return sep.join(str(int(v)) if ints else _num(rng, v) for v in vals)
+
+    def shape():
+        parts = []
+        if rng.random() < 0.7:
+            app = []
+            if rng.random() < 0.8:
+                if mat_defs and rng.random() < 0.3:
+                    app.append(f"<Material USE={q(mat_defs[int(rng.integers(len(mat_defs)))])}/>")
+                else:
+                    attrs = []
+                    for key in ("diffuseColor", "specularColor", "emissiveColor"):
+                        if rng.random() < 0.6:
+                            attrs.append(f"{key}={q(nums(rng.uniform(0, 1, 3)))}")
+                    if rng.random() < 0.5:
+                        attrs.append(f"shininess={q(_num(rng, rng.uniform(0, 1)))}")
+                    if rng.random() < 0.3:
+                        name = f"M{len(mat_defs)}"
+                        mat_defs.append(name)
+                        attrs.append(f"DEF={q(name)}")
+                    app.append("<Material " + " ".join(attrs) + "/>")
+            if rng.random() < 0.3:
+                url = f"xrand{seed}.png" if rng.random() < 0.7 else "nosuch.png"
+                app.append(f"<ImageTexture url={q(url)}/>")
+            parts.append("<Appearance>" + "".join(app) + "</Appearance>")
+        kind = rng.random()
+        if kind < 0.9:
+            if coord_defs and rng.random() < 0.25:
+                use = list(coord_defs)[int(rng.integers(len(coord_defs)))]
+                nv = coord_defs[use]
+                coord = f"<Coordinate USE={q(use)}/>"
+            else:
+                nv = int(rng.integers(3, 30))
+                dname = ""
+                if rng.random() < 0.3:
+                    name = f"C{len(coord_defs)}"
+                    coord_defs[name] = nv
+                    dname = f" DEF={q(name)}"
+                coord = f"<Coordinate{dname} point={q(nums(rng.uniform(-2, 2, 3 * nv)))}/>"
+            inner = [coord]
+            nn = int(rng.integers(1, 20))
+            nt = int(rng.integers(1, 20))
+            has_n, has_t = rng.random() < 0.5, rng.random() < 0.4
+            if has_n:
+                inner.append(f"<Normal vector={q(nums(rng.normal(size=3 * nn)))}/>")
+            if has_t:
+                inner.append(f"<TextureCoordinate point={q(nums(rng.uniform(0, 1, 2 * nt)))}/>")
+            if kind < 0.6:
+                polys = [rng.choice(nv, int(rng.integers(3, min(5, nv) + 1)), replace=False)
+                         for _ in range(int(rng.integers(1, 12)))]
+
+                def flat(lists, trailing):
+                    out = []
+                    for k, p in enumerate(lists):
+                        out += list(p)
+                        if k + 1 < len(lists) or trailing:
+                            out.append(-1)
+                    return out
+                attrs = [f"coordIndex={q(nums(flat(polys, rng.random() < 0.5), True))}"]
+                if has_n and rng.random() < 0.6:
+                    attrs.append(f"normalIndex={q(nums(flat([rng.integers(0, nn, len(p)) for p in polys], rng.random() < 0.5), True))}")
+                if has_t and rng.random() < 0.6:
+                    attrs.append(f"texCoordIndex={q(nums(flat([rng.integers(0, nt, len(p)) for p in polys], True), True))}")
+                parts.append("<IndexedFaceSet " + " ".join(attrs) + ">" + "".join(inner) + "</IndexedFaceSet>")
+            else:
+                idx = rng.integers(0, nv, 3 * int(rng.integers(1, 12)))
+                parts.append(f"<IndexedTriangleSet index={q(nums(idx, True))}>" + "".join(inner) +
+                             "</IndexedTriangleSet>")
+        return "<Shape>" + "".join(parts) + "</Shape>"
+
+    def item(depth):
+        if depth < 3 and rng.random() < 0.4:
+            tag = "Transform" if rng.random() < 0.7 else "Group"
+            attrs = []
+            if rng.random() < 0.6:
+                attrs.append(f"translation={q(nums(rng.uniform(-3, 3, 3), spaced=True))}")
+            if rng.random() < 0.6:
+                axis = rng.normal(size=3)
+                attrs.append(f"rotation={q(nums(list(axis) + [rng.uniform(-3, 3)], spaced=True))}")
+            if rng.random() < 0.5:
+                attrs.append(f"scale={q(nums(rng.uniform(0.2, 3, 3), spaced=True))}")
+            kids = "\n".join(item(depth + 1) for _ in range(int(rng.integers(0, 4))))
+            return f"<{tag} " + " ".join(attrs) + ">\n" + kids + f"\n</{tag}>"
+        if rng.random() < 0.08:
+            return "<!-- skipped -->" if rng.random() < 0.5 else "<Viewpoint position='0 0 10'/>"
+        return shape()
+
+    body = "\n".join(item(0) for _ in range(int(rng.integers(1, 5))))
+    name = f"xrand{seed}.x3d"
+    with open(os.path.join(d, name), "w") as f:
+        f.write('<?xml version="1.0" encoding="UTF-8"?>\n<X3D profile="Interchange">\n<Scene>\n' + body +
+                "\n</Scene>\n</X3D>\n")
     return name

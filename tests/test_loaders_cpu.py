@@ -227,3 +227,15 @@ def test_random_ascii_stl_matches_reference(tmp_path, product_lib, ref_lib, seed
     got = product_model(p)
     assert ref is not None and got is not None
     assert canonical(got) == canonical(ref)
+
+
+@pytest.mark.parametrize("seed", range(32))
+def test_random_x3d_matches_reference(tmp_path, product_lib, ref_lib, seed):
+    """Seeded random X3D scenes (tests/loader_files.random_x3d): the same
+    scene tree, transforms, arrays and materials as the reference's reader."""
+    name = loader_files.random_x3d(str(tmp_path), seed)
+    p = str(tmp_path / name)
+    ref = O.ref_load_mesh(p)
+    got = product_model(p)
+    assert ref is not None and got is not None
+    assert canonical(got) == canonical(ref)
