@@ -345,3 +345,48 @@ def random_scene(seed: int):
                     save_normals=rng.random() < 0.3)
     sc.ambientLight = np.float32(st.ambient)  # Renderer::render reads the scene's (src/Renderer.cpp:322)
     return st, sc
+
+
+def random_paints(seed: int):
+    """Seeded random paintMesh / paintTriangle sequence over a random scene's
+    camera: meshes of that scene painted with new transforms and materials
+    (textured or not), runs of view-space triangles with near-plane clipping
+    (world = true) and without (world = false), some crossing the near plane
+    or lying behind it, random windings.  Returns (state, paints)."""
+    from minirender_gb300.scene import Paint, Vertex, append_triangle, triangle_paint
+    st, sc = random_scene(seed)
+    rng = np.random.default_rng(5000 + seed)
+    meshes = []
+    stack = [sc]
+    while stack:
+        n = stack.pop()
+        if isinstance(n, TriMesh):
+            meshes.append(n)
+        stack.extend(n.children)
+    P = np.asarray(st.projection, np.float32).reshape(4, 4)
+    persp = P[3, 3] == 0
+    zlo = -10.0 if persp else -40.0
+
+    def material():
+        tex = rng.integers(0, 256, (int(rng.integers(1, 20)), int(rng.integers(1, 20)), 3)).astype(np.uint8) \
+            if rng.random() < 0.4 else None
+        return Material(diffuse=rng.uniform(0, 1, 3), specular=rng.uniform(0, 1, 3),
+                        emissive=rng.uniform(0, 0.2, 3), shininess=float(rng.uniform(0, 50)), texture=tex)
+
+    def vertex():
+        z = float(rng.uniform(zlo, 0.3))
+        s = abs(z) * 0.6 if persp else 3.5
+        return Vertex((rng.uniform(-s, s), rng.uniform(-s, s), z), rng.normal(size=3), rng.uniform(0, 3, 2))
+
+    paints = []
+    for _ in range(int(rng.integers(1, 7))):
+        if meshes and rng.random() < 0.5:
+            m = meshes[int(rng.integers(len(meshes)))]
+            xf = pj.mat_mul(pj.translate(*rng.uniform(-0.5, 0.5, 3)), pj.rotate_z(float(rng.uniform(-1, 1))))
+            paints.append(Paint(m, xf, material() if rng.random() < 0.7 else (m.material or Material())))
+        else:
+            p = triangle_paint(vertex(), vertex(), vertex(), material(), bool(rng.random() < 0.6))
+            for _ in range(int(rng.integers(0, 12))):
+                append_triangle(p, vertex(), vertex(), vertex())
+            paints.append(p)
+    return st, paints

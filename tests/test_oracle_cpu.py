@@ -166,3 +166,17 @@ def test_paints_match_golden():
         got = O.render_paints(st, paints)
         for k in ("image", "depth"):
             assert hashlib.sha256(got[k].tobytes()).hexdigest() == want[f"clear{int(clear)}"][k], (clear, k)
+
+
+@pytest.mark.parametrize("seed", range(32))
+def test_random_paints_vs_reference(ref_lib, seed):
+    """Seeded random paintMesh / paintTriangle sequences
+    (tests/edge_scenes.random_paints): the restatement equals the reference's
+    Renderer after render() and after clear()."""
+    import edge_scenes as E
+    st, paints = E.random_paints(seed)
+    got = O.render_paints(st, paints)
+    for clear in (False, True):
+        ref = O.ref_paint(st, paints, clear=clear)
+        assert _bits_equal(got["depth"], ref["depth"]), clear
+        assert _bits_equal(got["image"], ref["image"]), clear
