@@ -114,10 +114,12 @@ def tune(ctx: capi.Context, prepared, key: str, candidates: Sequence[Tuple[int, 
     best["table"] = table
     apply(ctx, best)
     cache[key] = best
-    try:
+    try:  # written whole, then renamed: a concurrent reader never sees half a file
         os.makedirs(os.path.dirname(path), exist_ok=True)
-        with open(path, "w") as f:
+        tmp = f"{path}.{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
             json.dump(cache, f, indent=1)
+        os.replace(tmp, path)
     except OSError:
         pass
     return best
