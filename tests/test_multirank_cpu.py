@@ -57,3 +57,8 @@ def test_reference_arm_under_torchrun():
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["cpu_baseline"]["kind"] == "port" and d["e2e"]["h2d_bytes_per_step"] == 0
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+              "scaling", "vs_baseline", "dtype", "data", "config", "e2e", "cpu_baseline"):
+        assert k in d, k
+    assert d["steps"] == 1 and d["warmup"] == 3 and d["metric"] == d["unit"] == "frames/s"
+    assert d["config"]["workload"] and d["cpu_baseline"]["cores"] >= 1 and d["cpu_baseline"]["sample"]
