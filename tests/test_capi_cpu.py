@@ -111,6 +111,20 @@ def test_collect_shapes_matches_oracle(product_lib, oracle_lib):
             C.string_at(C.addressof(b), C.sizeof(abi.mr_renderable) * nb)
 
 
+def test_collect_shapes_random_trees_match_oracle(product_lib, oracle_lib):
+    """Nested groups, meshes under meshes and instanced meshes of the seeded
+    random scenes: the library's collectShapes equals the oracle's bytes."""
+    import edge_scenes as E
+    for seed in range(48):
+        st, sc = E.random_scene(seed)
+        flat = S.flatten(sc)
+        a, na = capi.collect_shapes(flat.nodes)
+        b, nb = O.collect_shapes(flat)
+        assert na == nb >= 1
+        assert C.string_at(C.addressof(a), C.sizeof(abi.mr_renderable) * na) == \
+            C.string_at(C.addressof(b), C.sizeof(abi.mr_renderable) * nb), seed
+
+
 def test_collect_shapes_rejects_bad_trees(product_lib):
     nodes = (abi.mr_node * 2)()
     nodes[0].parent = -1
