@@ -33,8 +33,9 @@ def cases():
 
 def loader_digests():
     """tests/golden/loaders.json: digests of the reference loaders' output
-    (src/io.cpp, src/x3d.cpp) for the seeded sample files of
-    tests/loader_files.py, serialised as tests/test_loaders_cpu.py does."""
+    (src/io.cpp, src/x3d.cpp) for the seeded sample files and the seeded
+    random files of tests/loader_files.py, serialised as
+    tests/test_loaders_cpu.py does."""
     import json
     import tempfile
 
@@ -42,6 +43,9 @@ def loader_digests():
     import test_loaders_cpu as T
     with tempfile.TemporaryDirectory() as d:
         out = {n: T.digest(O.ref_load_mesh(os.path.join(d, n))) for n in loader_files.write_all(d)}
+    for key, make in T.RANDOM_FILES:
+        with tempfile.TemporaryDirectory() as d:
+            out[key] = T.digest(O.ref_load_mesh(os.path.join(d, make(d))))
     with open(os.path.join(HERE, "loaders.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print("loaders.json:", ", ".join(sorted(out)))

@@ -98,6 +98,13 @@ def _golden():
         return json.load(f)
 
 
+# (digest key, writer) of the seeded random files whose reference digests
+# tests/golden/make_golden.py records
+RANDOM_FILES = ([(f"random_obj/{s}", lambda d, s=s: loader_files.random_obj(d, s)) for s in range(8)] +
+                [(f"random_stl/{s}", lambda d, s=s: loader_files.random_ascii_stl(d, s)) for s in range(4)] +
+                [(f"random_x3d/{s}", lambda d, s=s: loader_files.random_x3d(d, s)) for s in range(8)])
+
+
 def test_models_match_golden(files, product_lib):
     d, names = files
     g = _golden()
@@ -284,3 +291,12 @@ def test_mutated_files_never_crash(tmp_path, product_lib):
         else:
             assert rc in (abi.MR_E_IO, abi.MR_E_INVALID, abi.MR_E_NOMEM), (n, k, rc)
     assert loaded > 100
+
+
+@pytest.mark.parametrize("key", [k for k, _ in RANDOM_FILES])
+def test_random_models_match_golden(tmp_path, product_lib, key):
+    """Seeded random files against digests of the reference loaders' output
+    (no reference build needed)."""
+    make = dict(RANDOM_FILES)[key]
+    name = make(str(tmp_path))
+    assert digest(product_model(str(tmp_path / name))) == _golden()[key]
