@@ -54,7 +54,8 @@ def loader_digests():
 def paint_digests():
     """tests/golden/paints.json: digests of the reference Renderer's image and
     depth for the paintMesh / paintTriangle sequence of
-    tests/edge_scenes.paint_sequence, after render() and after clear()."""
+    tests/edge_scenes.paint_sequence, after render() and after clear(), and
+    for the seeded random sequences of tests/edge_scenes.random_paints."""
     import hashlib
     import json
     st, paints = E.paint_sequence()
@@ -62,6 +63,9 @@ def paint_digests():
     for clear in (False, True):
         r = O.ref_paint(st, paints, clear=clear)
         out[f"clear{int(clear)}"] = {k: hashlib.sha256(r[k].tobytes()).hexdigest() for k in ("image", "depth")}
+    for seed in range(8):  # tests/edge_scenes.random_paints, after clear()
+        r = O.ref_paint(*E.random_paints(seed), clear=True)
+        out[f"random/{seed}"] = {k: hashlib.sha256(r[k].tobytes()).hexdigest() for k in ("image", "depth")}
     with open(os.path.join(HERE, "paints.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print("paints.json:", ", ".join(sorted(out)))

@@ -180,3 +180,17 @@ def test_random_paints_vs_reference(ref_lib, seed):
         ref = O.ref_paint(st, paints, clear=clear)
         assert _bits_equal(got["depth"], ref["depth"]), clear
         assert _bits_equal(got["image"], ref["image"]), clear
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_random_paints_match_golden(seed):
+    """Random paint sequences against the committed digests of the
+    reference's Renderer (tests/golden/paints.json; no reference build needed)."""
+    import hashlib
+    import json
+    import edge_scenes as E
+    with open(os.path.join(GOLDEN, "paints.json")) as f:
+        want = json.load(f)[f"random/{seed}"]
+    got = O.render_paints(*E.random_paints(seed))
+    for k in ("image", "depth"):
+        assert hashlib.sha256(got[k].tobytes()).hexdigest() == want[k], k
