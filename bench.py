@@ -105,7 +105,7 @@ class Clocks:
                 stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
-        except Exception:
+        except OSError:  # no nvidia-smi on this machine
             self.proc = None
 
     def _read(self):
@@ -119,7 +119,7 @@ class Clocks:
         self.proc.terminate()
         try:
             self.proc.wait(timeout=5)
-        except Exception:
+        except subprocess.TimeoutExpired:
             self.proc.kill()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
