@@ -61,6 +61,17 @@ def test_struct_layouts_match_ctypes(tmp_path):
     assert got == want
 
 
+@pytest.mark.parametrize("lang", ["c99", "c++11"])
+def test_header_compiles_strictly(tmp_path, lang):
+    """A plain C or C++ consumer (an FFI stub, a cgo preamble) includes the
+    header with every warning as an error."""
+    ext, cc = (".c", "gcc") if lang == "c99" else (".cpp", "g++")
+    src = tmp_path / ("h" + ext)
+    src.write_text('#include "minirender_gpu.h"\nint main(void) { return MR_ABI_VERSION > 0 ? 0 : 1; }\n')
+    subprocess.run([cc, f"-std={lang}", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-o", str(tmp_path / "h")], check=True)
+
+
 def test_abi_version_and_status(product_lib):
     assert product_lib.mr_abi_version() == 2
     assert product_lib.mr_status_string(abi.MR_E_BAD_INDEX) == b"mesh index out of range"
