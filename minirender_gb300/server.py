@@ -49,7 +49,11 @@ class RenderServer:
         q.material.texture = -1
         tex = texture if texture is not None else (m.texture if m is not None else None)
         if tex is not None and texture_key:
-            tex = np.ascontiguousarray(tex, np.uint8)
+            tex = np.asarray(tex)
+            if tex.dtype != np.uint8 or tex.ndim != 3 or tex.shape[2] != 3:
+                # requests carry RGB8 textures only; a cast would silently change float texels
+                raise TypeError("render-server textures are (rows, cols, 3) uint8 RGB8 arrays")
+            tex = np.ascontiguousarray(tex)
             q.texture_key = texture_key
             q.texture_rgb8 = tex.ctypes.data
             q.tex_rows, q.tex_cols = tex.shape[0], tex.shape[1]
