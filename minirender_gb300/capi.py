@@ -120,6 +120,7 @@ class Context:
             raise MRError(rc, "mr_create: " + lib().mr_status_string(rc).decode())
         self.h = h
         self._frame_hw = None
+        self._tex_layout = {}  # texture handle -> (dtype, shape) the library reads on update
 
     def _check(self, rc: int, what: str) -> int:
         if rc != 0:
@@ -166,6 +167,8 @@ class Context:
 
     def upload_texture(self, tex: np.ndarray) -> int:
         out = _I()
+        if tex.ndim != 3 or tex.shape[2] != 3:
+            raise ValueError(f"textures are (rows, cols, 3) arrays, got shape {tex.shape}")
         if tex.dtype == np.uint8:
             t = np.ascontiguousarray(tex)
             rc = lib().mr_texture_upload_rgb8(self.h, _ptr(t), t.shape[0], t.shape[1], C.byref(out))
@@ -173,13 +176,21 @@ class Context:
             t = np.ascontiguousarray(tex, np.float32)
             rc = lib().mr_texture_upload_f32(self.h, _ptr(t), t.shape[0], t.shape[1], C.byref(out))
         self._check(rc, "mr_texture_upload")
+        self._tex_layout[out.value] = (t.dtype, t.shape)
         return out.value
 
     def update_texture(self, handle: int, tex: np.ndarray):
+        """Re-sends a texture's texels; the library reads rows x cols x 3
+        elements of the upload's type from the array, so it must match."""
+        want = self._tex_layout.get(handle)
+        if want is not None and (tex.dtype != want[0] or tex.shape != want[1] or not tex.flags.c_contiguous):
+            raise ValueError(f"texture {handle} was uploaded as {want[1]} {want[0]}; "
+                             f"got {tex.shape} {tex.dtype} (contiguous: {tex.flags.c_contiguous})")
         self._check(lib().mr_texture_update(self.h, handle, _ptr(tex)), "mr_texture_update")
 
     def free_texture(self, handle: int):
         self._check(lib().mr_texture_free(self.h, handle), "mr_texture_free")
+        self._tex_layout.pop(handle, None)
 
     def render(self, frame: abi.mr_frame, renderables, n: int, outputs: int = abi.MR_OUT_DEFAULT):
         self._frame_hw = (frame.height, frame.width)

@@ -14,3 +14,18 @@ def test_non_rgb8_texture_is_refused(tex):
     st, sc = W.config1(32, 24)
     with pytest.raises(TypeError):
         srv.submit(st, sc.children[0], mesh_key=1, texture=tex, texture_key=2)
+
+
+def test_context_texture_layout_checks():
+    """Context.upload_texture / update_texture refuse arrays the library
+    would read past (checked before any device call)."""
+    from minirender_gb300 import capi
+    ctx = capi.Context.__new__(capi.Context)  # no device
+    ctx.h = None
+    ctx._tex_layout = {7: (np.dtype(np.uint8), (4, 5, 3))}
+    with pytest.raises(ValueError):
+        ctx.upload_texture(np.zeros((4, 5), np.uint8))
+    for bad in (np.zeros((4, 5, 3), np.float32), np.zeros((5, 4, 3), np.uint8),
+                np.zeros((4, 10, 3), np.uint8)[:, ::2]):
+        with pytest.raises(ValueError):
+            ctx.update_texture(7, bad)
