@@ -230,6 +230,13 @@ class Context:
         """Queues the D2H of RGB8, depth (and triangle ids) into caller-owned
         (pinned, for an asynchronous copy) arrays; wait() -- or the next
         read, render or stats call -- completes it."""
+        if self._frame_hw is not None:  # the library writes a whole frame into each array
+            H, W = self._frame_hw
+            for a, dt, n, name in ((rgb8, np.uint8, 3 * H * W, "rgb8"), (depth, np.float32, H * W, "depth"),
+                                   (tri_id, np.uint32, H * W, "tri_id")):
+                if a is not None and (a.dtype != dt or a.size != n or not a.flags.c_contiguous):
+                    raise ValueError(f"{name}: want {n} contiguous {np.dtype(dt)}, got {a.size} {a.dtype} "
+                                     f"(contiguous: {a.flags.c_contiguous})")
         self._check(lib().mr_read_async(self.h, _ptr(rgb8), _ptr(depth), None, _ptr(tri_id), None),
                     "mr_read_async")
 

@@ -29,3 +29,16 @@ def test_context_texture_layout_checks():
                 np.zeros((4, 10, 3), np.uint8)[:, ::2]):
         with pytest.raises(ValueError):
             ctx.update_texture(7, bad)
+
+
+def test_read_async_target_checks():
+    """read_async refuses targets smaller than the frame or of the wrong type."""
+    from minirender_gb300 import capi
+    ctx = capi.Context.__new__(capi.Context)  # no device
+    ctx.h = None
+    ctx._frame_hw = (6, 8)
+    ok8, okd = np.zeros((6, 8, 3), np.uint8), np.zeros((6, 8), np.float32)
+    for bad in ((np.zeros((6, 7, 3), np.uint8), okd), (ok8, np.zeros((6, 8), np.float64)),
+                (ok8, okd, np.zeros((6, 8), np.int64)), (np.zeros((8, 6, 6), np.uint8)[:, :, ::2], okd)):
+        with pytest.raises(ValueError):
+            ctx.read_async(*bad)
