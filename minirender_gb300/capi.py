@@ -199,9 +199,14 @@ class Context:
         self._check(lib().mr_render(self.h, C.byref(frame), C.addressof(renderables) if n else None,
                                     n, outputs), "mr_render")
 
+    def _hw(self):
+        if self._frame_hw is None:
+            raise RuntimeError("no frame has been rendered on this context")
+        return self._frame_hw
+
     def read(self, rgb8=True, depth=True, rgb_f32=False, tri_id=True, normals=False,
              allow_bad_index: bool = False) -> dict:
-        H, W = self._frame_hw
+        H, W = self._hw()
         out = {}
         if rgb8:
             out["rgb8"] = np.empty((H, W, 3), np.uint8)
@@ -249,7 +254,7 @@ class Context:
         return rc
 
     def range_image(self) -> np.ndarray:
-        H, W = self._frame_hw
+        H, W = self._hw()
         out = np.empty((H, W, 3), np.float32)
         self._check(lib().mr_read_range_image(self.h, _ptr(out)), "mr_read_range_image")
         return out

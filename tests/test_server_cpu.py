@@ -42,3 +42,14 @@ def test_read_async_target_checks():
                 (ok8, okd, np.zeros((6, 8), np.int64)), (np.zeros((8, 6, 6), np.uint8)[:, :, ::2], okd)):
         with pytest.raises(ValueError):
             ctx.read_async(*bad)
+
+
+def test_read_before_render_is_an_error():
+    from minirender_gb300 import capi
+    ctx = capi.Context.__new__(capi.Context)  # no device
+    ctx.h = None
+    ctx._frame_hw = None
+    with pytest.raises(RuntimeError):
+        ctx.read()
+    with pytest.raises(RuntimeError):
+        ctx.range_image()
