@@ -1,5 +1,6 @@
-"""Host-side request checks of the render server mirror
-(minirender_gb300/server.py) that run before any device call."""
+"""Host-side argument checks of the Python mirrors that run before any
+device call: render-server requests (minirender_gb300/server.py) and the
+context's texture and read targets (minirender_gb300/capi.py)."""
 import numpy as np
 import pytest
 
