@@ -335,8 +335,8 @@ MR_API int mr_server_destroy(mr_server* srv);
  * device memory, or a real-time loop that cannot afford cudaMalloc/cudaFree
  * and the device-wide synchronisation cudaFree implies.  Renders one mesh
  * (one renderable of Renderer::render, src/Renderer.cpp:311-381) with every
- * piece of working memory -- visibility buffer, counters, tile table,
- * per-triangle index-check mask, renderable record -- taken from one
+ * piece of working memory -- visibility buffer, counters, per-triangle
+ * index-check mask, renderable record and triangle-base table -- taken from one
  * file-scope device array of MR_NOALLOC_SCRATCH_BYTES that the library
  * reserves on each GPU it is loaded on, until the process exits.
  *
@@ -348,9 +348,13 @@ MR_API int mr_server_destroy(mr_server* srv);
  * bytes decoded as b/255, or floats; NULL for none), and the outputs rgb8
  * (H*W*3), depth (H*W), tri_id (H*W), any of which may be NULL.  Results are
  * bit-identical to mr_render of the same renderable.
+ * Arguments (null arrays with non-zero counts, negative counts, short index
+ * arrays) are checked before any device work and give MR_E_INVALID.
  * The first call on a device looks up the scratch array's device address
  * (cudaGetSymbolAddress) with that device current; make that first call
- * before any stream capture.  The call is synchronous on `cuda_stream`
+ * before any stream capture.  The address is kept for the life of the
+ * process, so the device must not be reset (cudaDeviceReset) while the
+ * library is in use.  The call is synchronous on `cuda_stream`
  * (NULL = legacy default stream).  All calls in the process share the one
  * scratch array, which keeps the previous call's contents: calls whose GPU
  * work overlaps (other host threads, other streams) race on it and must be

@@ -316,20 +316,24 @@ static int copy_mesh(mr_ctx* c, MeshRec& m, const mr_mesh_desc* d, cudaStream_t 
   return MR_OK;
 }
 
-static int check_desc(mr_ctx* c, const mr_mesh_desc* d) {
-  if (!d) return fail(c, MR_E_INVALID, "null mesh descriptor");
+const char* mesh_desc_problem(const mr_mesh_desc* d) {
+  if (!d) return "null mesh descriptor";
   if (d->n_vertices < 0 || d->n_normals < 0 || d->n_texcoords < 0 || d->n_indices < 0 ||
       d->n_normalsI < 0 || d->n_texcoordsI < 0)
-    return fail(c, MR_E_INVALID, "negative count");
-  if (d->n_indices % 3) return fail(c, MR_E_INVALID, "index count is not a multiple of 3");
-  if (d->n_normalsI < d->n_indices) return fail(c, MR_E_INVALID, "normalsI shorter than indices");
+    return "negative count";
+  if (d->n_indices % 3) return "index count is not a multiple of 3";
+  if (d->n_normalsI < d->n_indices) return "normalsI shorter than indices";
   bool has_uv = d->n_texcoords > 0 && d->n_texcoordsI > 0;
-  if (has_uv && d->n_texcoordsI < d->n_indices)
-    return fail(c, MR_E_INVALID, "texcoordsI shorter than indices");
+  if (has_uv && d->n_texcoordsI < d->n_indices) return "texcoordsI shorter than indices";
   if ((d->n_vertices && !d->vertices) || (d->n_normals && !d->normals) ||
       (has_uv && (!d->texcoords || !d->texcoordsI)) || (d->n_indices && (!d->indices || !d->normalsI)))
-    return fail(c, MR_E_INVALID, "null array with non-zero count");
-  return MR_OK;
+    return "null array with non-zero count";
+  return nullptr;
+}
+
+static int check_desc(mr_ctx* c, const mr_mesh_desc* d) {
+  const char* why = mesh_desc_problem(d);
+  return why ? fail(c, MR_E_INVALID, why) : MR_OK;
 }
 
 static size_t mesh_bytes(const mr_mesh_desc* d, bool has_uv) {

@@ -198,6 +198,11 @@ inline int cuda_fail(mr_ctx* c, cudaError_t e, const char* what) {
 
 
 extern "C" {  // internal (not exported): defined inside the C-ABI translation unit
+// Why a mesh descriptor cannot be used (negative counts, an index count not a
+// multiple of 3, normalsI / texcoordsI shorter than indices, a null array
+// with a non-zero count), or null when it is well formed.  Checked before
+// any device work by every entry point that takes a descriptor.
+const char* mesh_desc_problem(const mr_mesh_desc* d);
 // Batch stages shared by mr_render_batch and the render server.
 int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_scenes, const mr_renderable* rs,
                 int32_t n_rs, int32_t outputs);

@@ -42,6 +42,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <utility>
 
 #include "raster.cuh"
@@ -1369,8 +1370,8 @@ cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev,
   if (ev) cudaEventRecord(ev[0], st);
   // The clear also brings vis[] into L2 (write-allocate), so the setup
   // kernel's atomics hit L2.
-  int cgrid = grid_for(npx, 256);
-  k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(
+  const int cgrid = std::min(grid_for(npx, 256), sm_count() * 16);
+  k_clear<<<cgrid, 256, 0, st>>>(
       F.vis, npx, reinterpret_cast<uint32_t*>(F.counters), (uint32_t)(sizeof(Counters) / 4), nullptr, 0,
       F.stage_src, F.stage_dst, F.stage_n16);
   if (staged) cudaEventRecord(staged, st);  // the staging block has been read
@@ -1426,8 +1427,8 @@ cudaError_t launch_batch(const BatchParams& B, int threads, int grid, uint32_t* 
     k_vertex<<<grid_for((size_t)B.g.n_verts + B.g.n_nrms, 256), 256, 0, st>>>(B.g, none, B.scenes);
   }
   if (B.small_max > 0 && B.n_px) {  // small triangles' visibility words of every scene
-    int cgrid = grid_for(B.n_px, 256);
-    k_clear<<<cgrid < 152 * 16 ? cgrid : 152 * 16, 256, 0, st>>>(B.vis, B.n_px, nullptr, 0, nullptr, 0, nullptr, nullptr, 0);
+    const int cgrid = std::min(grid_for(B.n_px, 256), sm_count() * 16);
+    k_clear<<<cgrid, 256, 0, st>>>(B.vis, B.n_px, nullptr, 0, nullptr, 0, nullptr, nullptr, 0);
   }
   if (ev) cudaEventRecord(ev[1], st);
   if (B.g.n_tris) {

@@ -10,25 +10,18 @@
 // g_scratch is a host-side stand-in in host code, not a device address: its
 // device address is looked up once per device (cudaGetSymbolAddress, with
 // that device current) on the first call there, and that address is what the
-// kernels receive.  Every call shares the array and inherits the previous
-// call's contents, so the counters and tile table are cleared each call; the
-// visibility buffer is cleared by the frame's own clear kernel and the index
-// mask is rewritten by the validation kernel.  Calls whose GPU work overlaps
-// race on the array.
+// kernels receive.  The address belongs to the device's primary context, so
+// the device must not be reset (cudaDeviceReset) while the library is in use.
+// Every call shares the array and inherits the previous call's contents, so
+// the counters are cleared each call; the visibility buffer is cleared by the
+// frame's own clear kernel and the index mask is rewritten by the validation
+// kernel.  Calls whose GPU work overlaps race on the array.
 #include <cuda_runtime.h>
 #include <string.h>
 
 #include <mutex>
 
-#include "host_math.h"
-#include "layout.h"
-
-namespace mrg {
-cudaError_t launch_validate(const DevMesh& M, uint32_t* bad, cudaStream_t st);
-cudaError_t launch_frame(const FrameParams& F, cudaStream_t st, cudaEvent_t* ev, cudaEvent_t staged = nullptr);
-}  // namespace mrg
-
-using namespace mrg;
+#include "internal.h"
 
 namespace {
 
@@ -72,17 +65,16 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
                                         const mr_material* mat, const void* texture, int32_t tex_rows,
                                         int32_t tex_cols, int32_t tex_is_rgb8, uint8_t* rgb8, float* depth,
                                         uint32_t* tri_id, void* cuda_stream) {
+  // every argument is checked before any device work: a null array with a
+  // non-zero count would otherwise reach the kernels as address 0
   if (!f || !d || !transform || !mat) return MR_E_INVALID;
   if (f->width <= 0 || f->height <= 0) return MR_E_INVALID;
+  if (mesh_desc_problem(d)) return MR_E_INVALID;
   if (f->width > MR_NOALLOC_MAX_SIDE || f->height > MR_NOALLOC_MAX_SIDE ||
       (int64_t)f->width * f->height > MR_NOALLOC_MAX_PIXELS)
     return MR_E_NOALLOC_LIMIT;
-  if (d->n_indices < 0 || d->n_indices % 3 || d->n_normalsI < d->n_indices || d->n_vertices < 0 ||
-      d->n_normals < 0 || d->n_texcoords < 0)
-    return MR_E_INVALID;
   if (d->n_indices / 3 > MR_NOALLOC_MAX_TRIANGLES) return MR_E_NOALLOC_LIMIT;
   const bool has_uv = d->n_texcoords > 0 && d->n_texcoordsI > 0;
-  if (has_uv && d->n_texcoordsI < d->n_indices) return MR_E_INVALID;
   if (texture && (tex_rows <= 0 || tex_cols <= 0)) return MR_E_INVALID;
 
   int dev = 0;

@@ -24,7 +24,8 @@ from minirender_gb300.frame import FrameState
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "_build", "libmr_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libmr_ref.so")
-REF_SRC = "/root/reference"
+# the reference checkout the pin build reads in place (MR_REFERENCE_SRC overrides)
+REF_SRC = os.environ.get("MR_REFERENCE_SRC", "/root/reference")
 
 _lib = None
 _ref = None

@@ -4,6 +4,9 @@ Bar (per frame): visible sub-triangle id and depth bits identical, RGB8
 within 1 LSB on at least 99.9% of pixels (the rest only from powf/sqrtf
 rounding), float colour within 1e-4 absolute wherever the winner matches.
 """
+import json
+import os
+
 import numpy as np
 
 from minirender_gb300 import abi
@@ -50,3 +53,16 @@ def assert_parity(stats: dict):
     assert stats["depth_equal"], stats
     assert stats["rgb8_within_1lsb"] >= RGB8_FRAC_MIN, stats
     assert stats["float_max_err"] <= FLOAT_ATOL or stats["rgb8_max_err"] <= 1, stats
+
+
+def report(stats, kind: str = "plain") -> None:
+    """Appends one case's figures to parity_<kind>.jsonl in the directory named
+    by MR_PARITY_REPORT_DIR (nothing is written when it is unset)."""
+    d = os.environ.get("MR_PARITY_REPORT_DIR")
+    if not d:
+        return
+    os.makedirs(d, exist_ok=True)
+    rows = stats if isinstance(stats, list) else [stats]
+    with open(os.path.join(d, f"parity_{kind}.jsonl"), "a") as f:
+        for s in rows:
+            f.write(json.dumps(s) + "\n")

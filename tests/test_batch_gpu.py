@@ -1,22 +1,16 @@
 """Batched rendering (mr_render_batch): every scene of a batch equals the
 oracle's render of that scene alone (bit-exact ids and depth, RGB8 within
 1 LSB), with and without CUDA-graph replay, for every tuning."""
-import json
-import os
-
 import numpy as np
 import pytest
 
 import edge_scenes as E
-from parity import assert_parity, compare
+from parity import assert_parity, compare, report
 from minirender_gb300 import projection as pj
 from minirender_gb300 import workloads as W
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
-
-REPORT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
-
 
 def _items():
     items = [W.config4_scene(s) for s in range(6)]
@@ -49,10 +43,7 @@ def _check_all(b, items, refs, tag):
         stats = compare(got, ref, f"batch_{tag}_{i}")
         out.append(stats)
         assert_parity(stats)
-    os.makedirs(REPORT, exist_ok=True)
-    with open(os.path.join(REPORT, "parity_batch.jsonl"), "a") as f:
-        for s in out:
-            f.write(json.dumps(s) + "\n")
+    report(out, "batch")
     return out
 
 

@@ -155,3 +155,44 @@ def test_no_device_is_reported_not_faked(product_lib):
     assert product_lib.mr_create(0, C.byref(h)) == abi.MR_E_NO_DEVICE
     with pytest.raises(capi.MRError):
         capi.Context(0)
+
+
+def _noalloc_call(lib, desc, width=64, height=48):
+    st, _ = W.config1(width, height)
+    frame = st.to_c()
+    mat = abi.mr_material()
+    xf = (C.c_float * 16)(*np.eye(4, dtype=np.float32).reshape(16))
+    return lib.mr_render_noalloc(C.byref(frame), C.byref(desc), C.addressof(xf), C.byref(mat),
+                                 None, 0, 0, 0, None, None, None, None)
+
+
+@pytest.mark.parametrize("field", ["vertices", "normals", "indices", "normalsI", "texcoords", "texcoordsI"])
+def test_noalloc_rejects_null_arrays_before_device_work(product_lib, field):
+    """mr_render_noalloc takes device pointers it cannot inspect: an array
+    given as NULL with a non-zero count is refused (MR_E_INVALID) before any
+    device work, as mr_mesh_upload refuses it, instead of reaching a kernel
+    as address 0.  The call returns before touching a device, so this runs
+    without a GPU."""
+    fake = 1 << 40  # never dereferenced: the checks run first
+    d = abi.mr_mesh_desc(fake, 3, fake, 3, fake, 3, fake, 3, fake, 3, fake, 3)
+    setattr(d, field, None)
+    assert _noalloc_call(product_lib, d) == abi.MR_E_INVALID
+
+
+@pytest.mark.parametrize("bad", [{"n_normalsI": -3}, {"n_texcoordsI": -3}, {"n_vertices": -1},
+                                 {"n_indices": 4, "n_normalsI": 4, "n_texcoordsI": 4},
+                                 {"n_normalsI": 0}, {"n_texcoordsI": 1}])
+def test_noalloc_rejects_bad_counts_before_device_work(product_lib, bad):
+    fake = 1 << 40
+    d = abi.mr_mesh_desc(fake, 3, fake, 3, fake, 3, fake, 3, fake, 3, fake, 3)
+    for k, v in bad.items():
+        setattr(d, k, v)
+    assert _noalloc_call(product_lib, d) == abi.MR_E_INVALID
+
+
+def test_noalloc_limits_checked_before_device_work(product_lib):
+    """Frames larger than the fixed scratch give MR_E_NOALLOC_LIMIT (an empty
+    mesh: nothing could be dereferenced even if the check were missing)."""
+    d = abi.mr_mesh_desc()
+    for w, h in ((abi.MR_NOALLOC_MAX_SIDE + 1, 16), (2048, 2048)):
+        assert _noalloc_call(product_lib, d, w, h) == abi.MR_E_NOALLOC_LIMIT

@@ -1,26 +1,14 @@
 """Device path vs the oracle on the benchmark configurations and edge cases
 (bit-exact ids and depth, RGB8 within 1 LSB on >= 99.9% of pixels)."""
-import json
-import os
-
 import numpy as np
 import pytest
 
 import edge_scenes as E
-from parity import assert_parity, compare, gpu_render
+from parity import assert_parity, compare, gpu_render, report
 from minirender_gb300 import workloads as W
 from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
-
-REPORT = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "gpurun_out")
-
-
-def _report(stats):
-    os.makedirs(REPORT, exist_ok=True)
-    with open(os.path.join(REPORT, "parity.jsonl"), "a") as f:
-        f.write(json.dumps(stats) + "\n")
-
 
 @pytest.fixture(scope="module")
 def renderer(product_lib):
@@ -36,7 +24,7 @@ def _check(name, st, sc, renderer, **kw):
     stats = compare(gpu, ref, name)
     if st.save_normals:
         stats["normals_max_err"] = float(np.abs(gpu["normals"] - ref["normals"]).max())
-    _report(stats)
+    report(stats)
     assert_parity(stats)
     return stats
 
@@ -193,7 +181,7 @@ def test_paint_mesh_and_triangles(renderer, clear):
     gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
            "rgb8": renderer.getImageRGB8()}
     stats = compare(gpu, O.render_paints(st, paints), f"paints_clear{int(clear)}")
-    _report(stats)
+    report(stats)
     assert_parity(stats)
     assert stats["covered"] > 5000
 
@@ -211,7 +199,7 @@ def test_paint_over_rendered_scene(renderer):
     gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
            "rgb8": renderer.getImageRGB8()}
     stats = compare(gpu, O.render_paints(st, tri_runs, base_scene=sc), "paints_over_scene")
-    _report(stats)
+    report(stats)
     assert_parity(stats)
 
 
@@ -228,3 +216,40 @@ def test_unknown_renderable_flags_rejected(renderer):
     rs[0].flags = 0
     renderer.ctx.render(frame, rs, n, renderer.outputs)
     renderer.setScene(Scene())
+
+
+def _range_cases():
+    """getRangeImage cases: a perspective frame whose far plane (3.5) cuts
+    through the visible sphere, so part of the covered pixels lie past
+    `fardepth` and read as zero; an orthographic frame with depth below zero;
+    and random scenes of both projections."""
+    from minirender_gb300 import projection as pj
+    st, sc = W.config1(160, 120)
+    st.projection = pj.projection_frustum(pj.deg2rad(45), np.float32(160) / np.float32(120), 0.1, 3.5)
+    yield "persp_far_cut", st, sc
+    yield "ortho_negative_z", *E.ALL["ortho_negative_z"]()
+    for seed in (1, 6, 11, 30):
+        yield f"random_{seed}", *E.random_scene(seed)
+
+
+@pytest.mark.parametrize("case", list(_range_cases()), ids=lambda c: c[0])
+def test_range_image(renderer, case):
+    """Renderer::getRangeImage (src/Renderer.cpp:388-415) on the device
+    (mr_read_range_image) equals the oracle's bit for bit.  Another frame with
+    a different projection and size is rendered on the same context first,
+    so the range pass must read the last frame's projection, not a stale
+    staged one."""
+    name, st, sc = case
+    other_st, other_sc = W.config2(level=4, width=200, height=150, tex_size=32)
+    gpu_render(other_st, other_sc, renderer)
+    gpu, r = gpu_render(st, sc, renderer)
+    got = r.getRangeImage()
+    ref = O.render(st, sc)
+    assert np.array_equal(gpu["depth"].view(np.uint32), ref["depth"].view(np.uint32))
+    want = O.range_image(st, ref["depth"])
+    assert got.shape == want.shape
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32)), name
+    if name == "persp_far_cut":
+        covered = ref["ids"] != 0xFFFFFFFF
+        zeroed = covered & np.all(want == 0, axis=-1)
+        assert zeroed.sum() > 100 and (covered & ~zeroed).sum() > 100

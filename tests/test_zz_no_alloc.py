@@ -2,10 +2,12 @@
 memory (a host framework whose pool owns the device, or a real-time loop that
 cannot pay for cudaMalloc/cudaFree).  It keeps its working memory in a fixed
 device array inside the library, so this test checks that its output equals
-the ordinary entry point's (mr_render through Renderer) on two calls in a
-row -- the second call starts from the scratch the first one left behind --
-for an untextured and a textured scene, and that oversized requests are
-refused before any device work.
+the ordinary entry point's (mr_render through Renderer) and the oracle's on
+two calls in a row -- the second call starts from the scratch the first one
+left behind -- for an untextured and a textured scene; that a mesh with an
+out-of-range index is reported and a good mesh right after it renders
+correctly (no stale index-check bits); that an empty mesh with no outputs
+succeeds; and that oversized requests are refused before any device work.
 
 This file is named to be collected last; it passes on its own in a fresh
 process as well as after the other tests.
@@ -17,6 +19,7 @@ import pytest
 
 from parity import RGB8_FRAC_MIN
 from minirender_gb300 import abi, capi
+from oracle import oracle as O
 from minirender_gb300 import scene as S
 from minirender_gb300 import workloads as W
 from minirender_gb300.renderer import Renderer
@@ -41,21 +44,30 @@ def _existing(st, sc):
         r.close()
 
 
-def _noalloc(st, sc, calls=2):
+def _device_mesh(mesh, indices=None):
+    import torch
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    arrays = {k: getattr(mesh, k) for k in ("vertices", "normals", "texcoords", "indices", "normalsI",
+                                            "texcoordsI")}
+    if indices is not None:
+        arrays["indices"] = indices
+    keep = {k: dev(a) for k, a in arrays.items() if a.size}
+    p = lambda k: keep[k].data_ptr() if k in keep else None  # noqa: E731
+    desc = abi.mr_mesh_desc(p("vertices"), mesh.vertices.shape[0], p("normals"), mesh.normals.shape[0],
+                            p("texcoords"), mesh.texcoords.shape[0], p("indices"), arrays["indices"].size,
+                            p("normalsI"), mesh.normalsI.size, p("texcoordsI"), mesh.texcoordsI.size)
+    return desc, keep
+
+
+def _noalloc(st, sc, calls=2, indices=None, expect=abi.MR_OK):
     import torch
     flat = S.flatten(sc)
     rs, n = capi.collect_shapes(flat.nodes)
     assert n == 1
     mesh = flat.meshes[rs[0].mesh]
-    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
-    keep = {k: dev(getattr(mesh, k)) for k in ("vertices", "normals", "texcoords", "indices",
-                                                "normalsI", "texcoordsI") if getattr(mesh, k).size}
-    p = lambda k: keep[k].data_ptr() if k in keep else None  # noqa: E731
-    desc = abi.mr_mesh_desc(p("vertices"), mesh.vertices.shape[0], p("normals"), mesh.normals.shape[0],
-                            p("texcoords"), mesh.texcoords.shape[0], p("indices"), mesh.indices.size,
-                            p("normalsI"), mesh.normalsI.size, p("texcoordsI"), mesh.texcoordsI.size)
+    desc, _keep = _device_mesh(mesh, indices)
     tex = flat.textures[0] if flat.textures else None
-    tex_d = dev(tex) if tex is not None else None
+    tex_d = torch.from_numpy(np.ascontiguousarray(tex)).cuda() if tex is not None else None
     H, W_ = st.height, st.width
     rgb8 = torch.empty((H, W_, 3), dtype=torch.uint8, device="cuda")
     depth = torch.empty((H, W_), dtype=torch.float32, device="cuda")
@@ -71,7 +83,7 @@ def _noalloc(st, sc, calls=2):
             tex.shape[0] if tex is not None else 0, tex.shape[1] if tex is not None else 0,
             int(tex is not None and tex.dtype == np.uint8),
             rgb8.data_ptr(), depth.data_ptr(), ids.data_ptr(), torch.cuda.current_stream().cuda_stream)
-        assert rc == abi.MR_OK, capi.lib().mr_status_string(rc)
+        assert rc == expect, capi.lib().mr_status_string(rc)
         outs.append({"rgb8": rgb8.cpu().numpy(), "depth": depth.cpu().numpy(),
                      "ids": ids.cpu().numpy().view(np.uint32)})
         rgb8.fill_(7)
@@ -80,27 +92,59 @@ def _noalloc(st, sc, calls=2):
     return outs
 
 
+def _same(got, want, what):
+    assert np.array_equal(got["ids"], want["ids"]), f"{what}: visible ids differ"
+    assert np.array_equal(got["depth"].view(np.uint32), want["depth"].view(np.uint32)), f"{what}: depth"
+    d = np.abs(got["rgb8"].astype(np.int16) - want["rgb8"].astype(np.int16)).max(-1)
+    assert (d <= 1).mean() >= RGB8_FRAC_MIN, f"{what}: rgb8"
+
+
 @pytest.mark.parametrize("name,case", list(_scenes()), ids=[n for n, _ in _scenes()])
 def test_noalloc_matches_existing_entry_point(product_lib, name, case):
     st, sc = case
     want = _existing(st, sc)
+    ref = O.render(st, sc)
     for k, got in enumerate(_noalloc(st, sc)):
-        assert np.array_equal(got["ids"], want["ids"]), f"call {k}: visible ids differ"
-        assert np.array_equal(got["depth"].view(np.uint32), want["depth"].view(np.uint32)), f"call {k}: depth"
-        d = np.abs(got["rgb8"].astype(np.int16) - want["rgb8"].astype(np.int16)).max(-1)
-        assert (d <= 1).mean() >= RGB8_FRAC_MIN, f"call {k}: rgb8"
+        _same(got, want, f"call {k} vs mr_render")
+        _same(got, ref, f"call {k} vs the oracle")
+
+
+def test_noalloc_bad_index_then_good_mesh(product_lib):
+    """One out-of-range index (found by the index check, which reads only the
+    caller's in-bounds index memory) gives MR_E_BAD_INDEX; the next call with
+    a good mesh of the same triangle count returns MR_OK with the output of
+    mr_render, so no stale index-check bit survives in the shared scratch."""
+    st, sc = W.config1(160, 120)
+    mesh = S.flatten(sc).meshes[0]
+    bad = mesh.indices.copy()
+    bad[7] = mesh.vertices.shape[0] + 11
+    _noalloc(st, sc, calls=1, indices=bad, expect=abi.MR_E_BAD_INDEX)
+    got = _noalloc(st, sc, calls=1)[0]
+    _same(got, _existing(st, sc), "good mesh after a bad one")
+
+
+def test_noalloc_empty_mesh_no_outputs(product_lib):
+    """Zero triangles and no output buffers: nothing to draw, MR_OK."""
+    import torch
+    st, _ = W.config1(64, 48)
+    frame = st.to_c()
+    xf = (C.c_float * 16)(*np.eye(4, dtype=np.float32).reshape(16))
+    rc = capi.lib().mr_render_noalloc(C.byref(frame), C.byref(abi.mr_mesh_desc()), C.addressof(xf),
+                                      C.byref(abi.mr_material()), None, 0, 0, 0, None, None, None,
+                                      torch.cuda.current_stream().cuda_stream)
+    assert rc == abi.MR_OK, capi.lib().mr_status_string(rc)
 
 
 def test_noalloc_rejects_oversized_requests(product_lib):
-    st, sc = W.config1()
-    flat = S.flatten(sc)
-    desc = flat.meshes[0].desc()
+    """Sizes beyond the fixed scratch are refused before any device work (an
+    empty mesh, so nothing could be dereferenced even if the check moved)."""
+    st, _ = W.config1()
     mat = abi.mr_material()
     xf = (C.c_float * 16)(*np.eye(4, dtype=np.float32).reshape(16))
     for w, h in ((abi.MR_NOALLOC_MAX_SIDE + 1, 16), (2048, 2048)):
         st.width, st.height = w, h
         frame = st.to_c()
-        rc = capi.lib().mr_render_noalloc(C.byref(frame), C.byref(desc), C.addressof(xf), C.byref(mat),
-                                          None, 0, 0, 0, None, None, None, None)
+        rc = capi.lib().mr_render_noalloc(C.byref(frame), C.byref(abi.mr_mesh_desc()), C.addressof(xf),
+                                          C.byref(mat), None, 0, 0, 0, None, None, None, None)
         assert rc == abi.MR_E_NOALLOC_LIMIT
     assert capi.lib().mr_status_string(abi.MR_E_NOALLOC_LIMIT).startswith(b"request exceeds")
