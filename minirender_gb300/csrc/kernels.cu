@@ -43,6 +43,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <type_traits>
 #include <utility>
 
 #include "raster.cuh"
@@ -599,13 +600,59 @@ __global__ void __launch_bounds__(256) k_vertex(Geo G, View V, const SceneRec* s
   }
 }
 
-// Small-triangle record staged in shared memory for the warp's cooperative raster.
+// Small-triangle records staged in shared memory for the warp's cooperative
+// raster, in two layouts: SmallRec (80 bytes, 16-byte aligned, copied with
+// vector accesses) and PackedRec (60 bytes: pixel coordinates in 16 bits, an
+// odd word stride so lanes touching different records still hit different
+// banks), which leaves more of the SM's L1 to a kernel that spills.
 struct __align__(16) SmallRec {
   float p0x, p0y, p2x, p2y, n1x, n1y, n2x, n2y, z0, z1, z2;
   uint32_t id;
   int x0, y0, x1, rows;
   uint32_t tag;  // target frame (batches: scene)
 };
+struct PackedRec {
+  float p0x, p0y, p2x, p2y, n1x, n1y, n2x, n2y, z0, z1, z2;
+  uint32_t id;
+  uint32_t tag;
+  uint32_t lo;  // x0 | y0 << 16
+  uint32_t hi;  // x1 | rows << 16
+};
+__device__ __forceinline__ void rec_put(SmallRec& q, const Setup& S, uint32_t id, uint32_t tag) {
+  q.p0x = S.p0.x; q.p0y = S.p0.y; q.p2x = S.p2.x; q.p2y = S.p2.y;
+  q.n1x = S.n1.x; q.n1y = S.n1.y; q.n2x = S.n2.x; q.n2y = S.n2.y;
+  q.z0 = S.z[0]; q.z1 = S.z[1]; q.z2 = S.z[2];
+  q.id = id;
+  q.x0 = S.x0; q.y0 = S.y0; q.x1 = S.x1;
+  q.rows = S.y1 - S.y0 + 1;
+  q.tag = tag;
+}
+__device__ __forceinline__ void rec_put(PackedRec& q, const Setup& S, uint32_t id, uint32_t tag) {
+  q.p0x = S.p0.x; q.p0y = S.p0.y; q.p2x = S.p2.x; q.p2y = S.p2.y;
+  q.n1x = S.n1.x; q.n1y = S.n1.y; q.n2x = S.n2.x; q.n2y = S.n2.y;
+  q.z0 = S.z[0]; q.z1 = S.z[1]; q.z2 = S.z[2];
+  q.id = id;
+  q.tag = tag;
+  // frame coordinates and small boxes' row counts fit 16 bits (sides <= 65536)
+  q.lo = (uint32_t)S.x0 | ((uint32_t)S.y0 << 16);
+  q.hi = (uint32_t)S.x1 | ((uint32_t)(S.y1 - S.y0 + 1) << 16);
+}
+__device__ __forceinline__ int rec_rows(const SmallRec& q) { return q.rows; }
+__device__ __forceinline__ int rec_rows(const PackedRec& q) { return (int)(q.hi >> 16); }
+template <class Rec>
+__device__ __forceinline__ Setup rec_get(const Rec& q) {
+  Setup U;
+  U.p0 = v2(q.p0x, q.p0y); U.p2 = v2(q.p2x, q.p2y);
+  U.n1 = v2(q.n1x, q.n1y); U.n2 = v2(q.n2x, q.n2y);
+  U.z[0] = q.z0; U.z[1] = q.z1; U.z[2] = q.z2;
+  if constexpr (sizeof(Rec) == sizeof(PackedRec)) {
+    U.x0 = (int)(q.lo & 0xffffu); U.y0 = (int)(q.lo >> 16); U.x1 = (int)(q.hi & 0xffffu);
+  } else {
+    U.x0 = q.x0; U.y0 = q.y0; U.x1 = q.x1;
+  }
+  return U;
+}
+constexpr int kStageRecs = 32;  // records staged per warp and round
 
 constexpr int kSetupThreads = 256;
 constexpr int kSetupWarps = kSetupThreads / 32;
@@ -627,112 +674,111 @@ struct BatchTarget {
   __device__ bool perspective(uint32_t sc) const { return scenes[sc].v.persp != 0; }
 };
 
-// Raster of the warp's small sub-triangles (kind 1) of triangle g, whose
-// frame is `tag`, with 64-bit atomicMin into the target (src/Renderer.cpp:
+// Raster of a sub-triangle whose bounding box spans at most 4x4 pixels by
+// one thread (src/Renderer.cpp:238-269): the row and column loops have
+// constant bounds and unroll, so the rows' independent edge evaluations
+// interleave (each row still starts from its bounding-box edge and steps
+// column by column).  row(y) gives the visibility words of row y.
+template <typename RowFn>
+__device__ __forceinline__ void raster_tiny(const Setup& Q, bool persp, uint32_t id, RowFn row_of) {
+#pragma unroll
+  for (int r = 0; r < 4; r++) {
+    const int y = Q.y0 + r;
+    if (y <= Q.y1) {
+      unsigned long long* row = row_of(y);
+      float e1, e2;
+      row_start(Q, y, e1, e2);
+#pragma unroll
+      for (int c = 0; c < 4; c++) {
+        const int x = Q.x0 + c;
+        if (x <= Q.x1 && covered(e1, e2)) {
+          float k0, k1, k2;
+          const float z = frag_depth(Q, persp, e1, e2, k0, k1, k2);
+          if (z < 1e11f) atomicMin(row + x, ((unsigned long long)depth_key(z) << 32) | id);
+        }
+        e1 += Q.n1.x;
+        e2 += Q.n2.x;
+      }
+    }
+  }
+}
+
+// Raster of the warp's small sub-triangles (kind 1; ids[s] the id of
+// sub-triangle s), whose frame is `tag`, with 64-bit atomicMin into the
+// target (src/Renderer.cpp:
 // 238-269).  When every one in the warp spans at most 4x4 pixels the lanes
 // rasterise their own (the loops are short and nearly uniform); otherwise
 // they are staged in shared memory and rasterised with one (triangle, row)
 // per lane so every lane has work.  Called by all lanes of the warp.
-template <class Target>
-__device__ __forceinline__ void raster_small(const Setup (&S)[2], const int (&kind)[2], uint32_t g, uint32_t tag,
-                                             const Target& T, SmallRec* s_rec, int* s_pre) {
+template <class Target, class Rec>
+__device__ __forceinline__ void raster_small(const Setup (&S)[2], const int (&kind)[2], const uint32_t (&ids)[2],
+                                             uint32_t tag, const Target& T, Rec* s_rec, int* s_pre) {
   const unsigned lane = threadIdx.x & 31, lt = (1u << lane) - 1u;
   int span = 0;
 #pragma unroll
   for (int s = 0; s < 2; s++)
     if (kind[s] == 1) span = max(span, max(S[s].x1 - S[s].x0, S[s].y1 - S[s].y0) + 1);
   if (__reduce_max_sync(0xffffffffu, (unsigned)span) <= 4u) {
-    // at most 4x4 pixels: the row and column loops have constant bounds and
-    // unroll, so the rows' independent edge evaluations interleave (each row
-    // still starts from its bounding-box edge and steps column by column)
 #pragma unroll
     for (int s = 0; s < 2; s++)
-      if (kind[s] == 1) {
-        const Setup& Q = S[s];
-        const uint32_t id = 2u * g + (uint32_t)s;
-        const bool persp = T.perspective(tag);
-#pragma unroll
-        for (int r = 0; r < 4; r++) {
-          const int y = Q.y0 + r;
-          if (y <= Q.y1) {
-            unsigned long long* row = T.row(tag, y);
-            float e1, e2;
-            row_start(Q, y, e1, e2);
-#pragma unroll
-            for (int c = 0; c < 4; c++) {
-              const int x = Q.x0 + c;
-              if (x <= Q.x1 && covered(e1, e2)) {
-                float k0, k1, k2;
-                const float z = frag_depth(Q, persp, e1, e2, k0, k1, k2);
-                if (z < 1e11f) atomicMin(row + x, ((unsigned long long)depth_key(z) << 32) | id);
-              }
-              e1 += Q.n1.x;
-              e2 += Q.n2.x;
-            }
-          }
-        }
-      }
+      if (kind[s] == 1)
+        raster_tiny(S[s], T.perspective(tag), ids[s], [&](int y) { return T.row(tag, y); });
     return;
   }
-  int n = 0;
+  // one round per sub-triangle slot (at most 32 records; slot 1 holds the
+  // second half of near-clipped triangles only)
 #pragma unroll
   for (int s = 0; s < 2; s++) {
-    unsigned m = __ballot_sync(0xffffffffu, kind[s] == 1);
-    if (kind[s] == 1) {
-      SmallRec& q = s_rec[n + __popc(m & lt)];
-      q.p0x = S[s].p0.x; q.p0y = S[s].p0.y; q.p2x = S[s].p2.x; q.p2y = S[s].p2.y;
-      q.n1x = S[s].n1.x; q.n1y = S[s].n1.y; q.n2x = S[s].n2.x; q.n2y = S[s].n2.y;
-      q.z0 = S[s].z[0]; q.z1 = S[s].z[1]; q.z2 = S[s].z[2];
-      q.id = 2u * g + (uint32_t)s;
-      q.x0 = S[s].x0; q.y0 = S[s].y0; q.x1 = S[s].x1;
-      q.rows = S[s].y1 - S[s].y0 + 1;
-      q.tag = tag;
-    }
-    n += __popc(m);
-  }
-  __syncwarp();
-  if (n == 0) return;
-  int c0 = (int)lane < n ? s_rec[lane].rows : 0;
-  int c1 = (int)lane + 32 < n ? s_rec[lane + 32].rows : 0;
+    const unsigned m = __ballot_sync(0xffffffffu, kind[s] == 1);
+    if (m == 0) continue;
+    const int n = __popc(m);
+    if (kind[s] == 1) rec_put(s_rec[__popc(m & lt)], S[s], ids[s], tag);
+    __syncwarp();
+    const int c = (int)lane < n ? rec_rows(s_rec[lane]) : 0;
+    int inc = c;
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    int u0 = __shfl_up_sync(0xffffffffu, c0, o), u1 = __shfl_up_sync(0xffffffffu, c1, o);
-    if ((int)lane >= o) { c0 += u0; c1 += u1; }
-  }
-  int tot0 = __shfl_sync(0xffffffffu, c0, 31), tot1 = __shfl_sync(0xffffffffu, c1, 31);
-  if (lane == 0) s_pre[0] = 0;
-  s_pre[lane + 1] = c0;
-  s_pre[lane + 33] = tot0 + c1;
-  __syncwarp();
-  const int total = tot0 + tot1;
-  for (int b = 0; b < total; b += 32) {
-    int k = b + (int)lane;
-    if (k < total) {
-      int lo = 0, hi = n;
-      while (hi - lo > 1) {
-        int mid = (lo + hi) >> 1;
-        if (s_pre[mid] <= k) lo = mid; else hi = mid;
-      }
-      const SmallRec& q = s_rec[lo];
-      Setup U;
-      U.p0 = v2(q.p0x, q.p0y); U.p2 = v2(q.p2x, q.p2y);
-      U.n1 = v2(q.n1x, q.n1y); U.n2 = v2(q.n2x, q.n2y);
-      U.z[0] = q.z0; U.z[1] = q.z1; U.z[2] = q.z2;
-      U.x0 = q.x0; U.x1 = q.x1; U.y0 = q.y0;
-      const int y = q.y0 + (k - s_pre[lo]);
-      unsigned long long* row = T.row(q.tag, y);
-      walk_row(U, T.perspective(q.tag), q.id, y, U.x0, U.x1,
-               [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, inc, o);
+      if ((int)lane >= o) inc += u;
     }
+    const int total = __shfl_sync(0xffffffffu, inc, 31);
+    s_pre[lane] = inc - c;
+    __syncwarp();
+    for (int b = 0; b < total; b += 32) {
+      const int k = b + (int)lane;
+      if (k < total) {
+        int lo = 0;  // the last record lo < n with s_pre[lo] <= k
+#pragma unroll
+        for (int step = 16; step; step >>= 1)
+          if (lo + step < n && s_pre[lo + step] <= k) lo += step;
+        const Rec& q = s_rec[lo];
+        const Setup U = rec_get(q);
+        const int y = U.y0 + (k - s_pre[lo]);
+        const uint32_t tg = q.tag;
+        unsigned long long* row = T.row(tg, y);
+        walk_row(U, T.perspective(tg), q.id, y, U.x0, U.x1,
+                 [&](int x, unsigned long long v, float, float) { atomicMin(row + x, v); });
+      }
+    }
+    __syncwarp();  // s_rec / s_pre free for the warp's next use
   }
-  __syncwarp();  // s_rec / s_pre free for the warp's next use
 }
 
+// Blocks per SM the register budget of k_setup must allow.  With the vertex
+// pass the kernel waits on index -> vertex gathers and more resident warps
+// hide that: 6 blocks (40 registers, some spilled to L1) with the packed
+// staging records, which leave more L1 to the spills.  Without it (triangle
+// soups) it is bound by instruction issue, spilling costs more than the
+// extra warps hide, and the aligned records' vector copies are cheaper: 4
+// blocks (64 registers).  Measured on 1080p and 4K frames.
 template <bool PRE>
-__global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
+constexpr int kSetupMinBlocks = PRE ? 6 : 4;
+template <bool PRE>
+__global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks<PRE>) k_setup(FrameParams F) {
   pdl_wait();
-  __shared__ SmallRec s_rec[kSetupWarps][64];
-  __shared__ int s_pre[kSetupWarps][65];
+  using Rec = std::conditional_t<PRE, PackedRec, SmallRec>;  // see kSetupMinBlocks
+  __shared__ Rec s_rec[kSetupWarps][kStageRecs];
+  __shared__ int s_pre[kSetupWarps][kStageRecs];
   __shared__ BlockCounters bc;
   if (threadIdx.x < 3) bc.v[threadIdx.x] = 0;
   __syncthreads();
@@ -797,7 +843,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup(FrameParams F) {
       }
     }
   }
-  raster_small(S, kind, g, 0u, FrameTarget{F.vis, F.v.W, persp}, s_rec[w], s_pre[w]);
+  const uint32_t ids[2] = {2u * g, 2u * g + 1u};
+  raster_small(S, kind, ids, 0u, FrameTarget{F.vis, F.v.W, persp}, s_rec[w], s_pre[w]);
   block_count(bc, 0, n_raster);
   block_count(bc, 1, n_small);
   block_count(bc, 2, n_clipped);
@@ -884,9 +931,9 @@ __global__ void __launch_bounds__(256, 4) k_resolve(FrameParams F) {
 // Setup of every triangle of every scene: each sub-triangle with pixels to
 // test becomes a record (warp-compacted), counted into its scene's tiles.
 template <bool PRE>
-__global__ void __launch_bounds__(kSetupThreads) k_setup_batch(BatchParams B) {
-  __shared__ SmallRec s_rec[kSetupWarps][64];
-  __shared__ int s_pre[kSetupWarps][65];
+__global__ void __launch_bounds__(kSetupThreads, 3) k_setup_batch(BatchParams B) {
+  __shared__ SmallRec s_rec[kSetupWarps][kStageRecs];
+  __shared__ int s_pre[kSetupWarps][kStageRecs];
   __shared__ BlockCounters bc;
   __shared__ unsigned s_fill, s_base;
   if (threadIdx.x < 3) bc.v[threadIdx.x] = 0;
@@ -941,7 +988,8 @@ __global__ void __launch_bounds__(kSetupThreads) k_setup_batch(BatchParams B) {
     }
     base += __popc(m);
   }
-  if (B.small_max > 0) raster_small(S, kind, g, scene, BatchTarget{B.scenes}, s_rec[w], s_pre[w]);
+  const uint32_t ids[2] = {2u * g, 2u * g + 1u};
+  if (B.small_max > 0) raster_small(S, kind, ids, scene, BatchTarget{B.scenes}, s_rec[w], s_pre[w]);
   block_count(bc, 0, n_raster);
   block_count(bc, 1, n_small);
   block_count(bc, 2, n_clipped);
