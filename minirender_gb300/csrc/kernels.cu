@@ -171,22 +171,47 @@ __device__ __forceinline__ void corners(const Geo& G, const DevRenderable& R, in
   }
 }
 
+// Corner record of a triangle (32 words, 128 bytes; DevMesh::rec):
+//   words 0-8   corner positions p0, p1, p2
+//   word 15     layout flag: kRecPerFace or 0
+// per-face layout (one normal index and one texcoord index for all three
+// corners, as in a soup with face normals: everything in the first 64 bytes)
+//   words 9-11  the normal, 12-13 the texcoord, 14 zero
+// per-corner layout
+//   words 9-11  n0, 12-14 n1, 16-18 n2, 19-24 uv0, uv1, uv2
+// Texcoords are zero for meshes without them.
+constexpr uint32_t kRecPerFace = 1u;
+
 // The view-space corners with attributes of triangle t from its corner
 // record: the same values corners<false, true> gathers (src/Renderer.cpp:
-// 344-348, 356-373).
+// 344-348, 356-373).  A per-face record needs its first 64 bytes only.
 __device__ __forceinline__ void corners_rec(const DevRenderable& R, int t, Vtx (&v)[3]) {
   const float4* r = R.mesh.rec + (size_t)8 * t;
-  float f[24];
+  const float4 q0 = __ldg(r), q1 = __ldg(r + 1), q2 = __ldg(r + 2), q3 = __ldg(r + 3);
+  v[0].pos = affine(R.mv, v3(q0.x, q0.y, q0.z));
+  v[1].pos = affine(R.mv, v3(q0.w, q1.x, q1.y));
+  v[2].pos = affine(R.mv, v3(q1.z, q1.w, q2.x));
+  const V3 n0 = v3(q2.y, q2.z, q2.w);
+  if (__float_as_uint(q3.w) == kRecPerFace) {
+    const V3 n = affine(R.nm, n0);
+    const V2 uv = R.mesh.has_uv ? v2(q3.x, q3.y) : v2(0, 0);
 #pragma unroll
-  for (int k = 0; k < 6; k++) {
-    const float4 q = __ldg(r + k);
-    f[4 * k] = q.x; f[4 * k + 1] = q.y; f[4 * k + 2] = q.z; f[4 * k + 3] = q.w;
-  }
-#pragma unroll
-  for (int c = 0; c < 3; c++) {
-    v[c].pos = affine(R.mv, v3(f[3 * c], f[3 * c + 1], f[3 * c + 2]));
-    v[c].nrm = affine(R.nm, v3(f[9 + 3 * c], f[9 + 3 * c + 1], f[9 + 3 * c + 2]));
-    v[c].uv = R.mesh.has_uv ? v2(f[18 + 2 * c], f[18 + 2 * c + 1]) : v2(0, 0);
+    for (int c = 0; c < 3; c++) {
+      v[c].nrm = n;
+      v[c].uv = uv;
+    }
+  } else {
+    const float4 q4 = __ldg(r + 4), q5 = __ldg(r + 5), q6 = __ldg(r + 6);
+    v[0].nrm = affine(R.nm, n0);
+    v[1].nrm = affine(R.nm, v3(q3.x, q3.y, q3.z));
+    v[2].nrm = affine(R.nm, v3(q4.x, q4.y, q4.z));
+    if (R.mesh.has_uv) {
+      v[0].uv = v2(q4.w, q5.x);
+      v[1].uv = v2(q5.y, q5.z);
+      v[2].uv = v2(q5.w, q6.x);
+    } else {
+      v[0].uv = v[1].uv = v[2].uv = v2(0, 0);
+    }
   }
 }
 
@@ -560,21 +585,41 @@ __global__ void k_validate(DevMesh M, uint32_t* bad, float4* rec) {
   unsigned m = __ballot_sync(0xffffffffu, b);
   if ((threadIdx.x & 31) == 0 && (t >> 5) < ((M.n_tri + 31) >> 5)) bad[t >> 5] = m;
   if (rec && t < M.n_tri && !b) {
-    float f[24];
+    // the layout of corners_rec
+    float f[28];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       f[3 * c + 0] = M.pos[3 * ip[c] + 0];
       f[3 * c + 1] = M.pos[3 * ip[c] + 1];
       f[3 * c + 2] = M.pos[3 * ip[c] + 2];
-      f[9 + 3 * c + 0] = M.nrm[3 * in[c] + 0];
-      f[9 + 3 * c + 1] = M.nrm[3 * in[c] + 1];
-      f[9 + 3 * c + 2] = M.nrm[3 * in[c] + 2];
-      f[18 + 2 * c + 0] = M.has_uv ? M.uv[2 * it[c] + 0] : 0.f;
-      f[18 + 2 * c + 1] = M.has_uv ? M.uv[2 * it[c] + 1] : 0.f;
     }
+    const bool per_face = in[0] == in[1] && in[1] == in[2] && it[0] == it[1] && it[1] == it[2];
     float4* r = rec + (size_t)8 * t;
+    if (per_face) {
+      f[9] = M.nrm[3 * in[0] + 0];
+      f[10] = M.nrm[3 * in[0] + 1];
+      f[11] = M.nrm[3 * in[0] + 2];
+      f[12] = M.has_uv ? M.uv[2 * it[0] + 0] : 0.f;
+      f[13] = M.has_uv ? M.uv[2 * it[0] + 1] : 0.f;
+      f[14] = 0.f;
+      f[15] = __uint_as_float(kRecPerFace);
 #pragma unroll
-    for (int k = 0; k < 6; k++) r[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+      for (int k = 0; k < 4; k++) r[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+    } else {
+      const int nw[3] = {9, 12, 16}, uw[3] = {19, 21, 23};
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        f[nw[c] + 0] = M.nrm[3 * in[c] + 0];
+        f[nw[c] + 1] = M.nrm[3 * in[c] + 1];
+        f[nw[c] + 2] = M.nrm[3 * in[c] + 2];
+        f[uw[c] + 0] = M.has_uv ? M.uv[2 * it[c] + 0] : 0.f;
+        f[uw[c] + 1] = M.has_uv ? M.uv[2 * it[c] + 1] : 0.f;
+      }
+      f[15] = 0.f;
+      f[25] = f[26] = f[27] = 0.f;
+#pragma unroll
+      for (int k = 0; k < 7; k++) r[k] = make_float4(f[4 * k], f[4 * k + 1], f[4 * k + 2], f[4 * k + 3]);
+    }
   }
 }
 

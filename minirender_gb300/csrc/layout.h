@@ -26,9 +26,10 @@ struct DevMesh {
   const int32_t* tidx;
   const uint32_t* bad;   // bit t set: triangle t has an index out of range
   // Soup-like meshes (3 * n_tri < 2 * n_pos): triangle t's corner positions,
-  // normals and texcoords gathered at upload into rec[8t .. 8t+5] (128 B per
-  // triangle; texcoords zero without uv), so a pixel's winner is read from
-  // one record instead of six scattered arrays.  Null otherwise.
+  // normals and texcoords gathered at upload into rec[8t .. 8t+7] (128 B per
+  // triangle; the first 64 B hold all of a triangle whose three corners share
+  // one normal and one texcoord), so a pixel's winner is read from one record
+  // instead of six scattered arrays.  Null otherwise.
   const float4* rec;
   int32_t n_pos, n_nrm, n_uv, n_tri;
   int32_t has_uv;       // texcoords and texcoordsI both non-empty
