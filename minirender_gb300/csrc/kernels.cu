@@ -141,6 +141,35 @@ __device__ __forceinline__ int clip_tri(float zn, Vtx (&v)[3], Vtx (&sub)[2][3])
   return 2;
 }
 
+// Sub-triangle s (0 or 1) of clipTriangle's output for a triangle that
+// crosses the near plane and has that sub-triangle, computed in place in v:
+// the same operations as clip_tri, without materialising both halves.
+template <bool ATTR>
+__device__ __forceinline__ void clip_pick(float zn, Vtx (&v)[3], int s) {
+  for (int it = 0; it < 3 && (v[0].pos.z < v[1].pos.z || v[0].pos.z < v[2].pos.z); it++) {
+    Vtx t0 = v[0]; v[0] = v[2]; v[2] = v[1]; v[1] = t0;
+  }
+  if (v[1].pos.z > zn) {
+    const Vtx a = clip_vtx<ATTR>(zn, v[0], v[2]);
+    v[1] = clip_vtx<ATTR>(zn, v[1], v[2]);
+    v[0] = a;
+    return;
+  }
+  if (v[2].pos.z > zn) {
+    const Vtx a = clip_vtx<ATTR>(zn, v[0], v[1]);
+    v[2] = clip_vtx<ATTR>(zn, v[1], v[2]);
+    v[0] = a;
+    return;
+  }
+  const Vtx v01 = clip_vtx<ATTR>(zn, v[0], v[1]);
+  if (s) {  // (v01, v2, v02)
+    const Vtx v02 = clip_vtx<ATTR>(zn, v[0], v[2]);
+    v[1] = v[2];
+    v[2] = v02;
+  }
+  v[0] = v01;
+}
+
 // View-space corners of triangle t (paintMesh, src/Renderer.cpp:344-379).
 template <bool PRE, bool ATTR>
 __device__ __forceinline__ void corners(const Geo& G, const DevRenderable& R, int t, const int (&ip)[3],
@@ -425,13 +454,7 @@ __device__ __forceinline__ const DevRenderable* winner_tri(const View& V, const 
   }
   const float zn = R->no_clip ? __int_as_float(0x7f800000) : V.znear;
   clipped = vc[0].pos.z > zn || vc[1].pos.z > zn || vc[2].pos.z > zn;
-  if (clipped) {
-    Vtx sub[2][3];
-    clip_tri<true>(zn, vc, sub);
-    // sub-triangle s exists: it won this pixel
-#pragma unroll
-    for (int c = 0; c < 3; c++) vc[c] = s ? sub[1][c] : sub[0][c];
-  }
+  if (clipped) clip_pick<true>(zn, vc, s);  // sub-triangle s exists: it won this pixel
   return R;
 }
 
@@ -1175,7 +1198,10 @@ __device__ __forceinline__ void raster_items(const BigRec* s_recs, const uint32_
 //      scene's outputs.
 // MINB: blocks of 256 threads per SM the register allocation must allow
 // (2: up to 128 registers per thread, for 64-thread blocks; 4: up to 64, so
-// that 128- and 256-thread blocks keep enough warps resident).
+// that 128- and 256-thread blocks keep enough warps resident).  At 64
+// registers the vertex-pass instance spills 216 bytes per thread; an 80-
+// register instance (3 blocks) that spills 36 was measured slower on the
+// 256-scene batch (fused stage 3.62 vs 3.37 ms), so the warps win.
 template <int MINB, bool PRE>
 __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* block_sums) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -1498,8 +1524,11 @@ size_t batch_smem(int tile_w, int tile_h, int chunk) {
          (size_t)(chunk + 1) * sizeof(uint32_t);
 }
 static const void* batch_kernel(int threads, bool pre) {
-  if (pre) return threads <= 64 ? (const void*)k_batch<2, true> : (const void*)k_batch<4, true>;
-  return threads <= 64 ? (const void*)k_batch<2, false> : (const void*)k_batch<4, false>;
+  if (pre)
+    return threads <= 64 ? (const void*)k_batch<2, true>
+                         : (const void*)k_batch<4, true>;
+  return threads <= 64 ? (const void*)k_batch<2, false>
+                       : (const void*)k_batch<4, false>;
 }
 // Co-resident blocks of k_batch for the given shape (its cooperative grid).
 int batch_grid(int tile_w, int tile_h, int chunk, int threads, bool pre) {
