@@ -63,21 +63,28 @@ def parse():
                    help="tile,threads,chunk or tile_w,tile_h,threads,chunk[,small_max] for batches "
                         "(skips the autotuner)")
     p.add_argument("--views", type=int, default=8, help="camera views per batched launch (config1-3)")
+    p.add_argument("--triangles", type=int, default=None,
+                   help="config3 only: soup size (default 10,000,000; smaller soups for profiler captures)")
+    p.add_argument("--size", default=None, help="config3 only: WxH frame (default 3840x2160)")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true", help="skip the end-to-end legs (profiling runs)")
+    p.add_argument("--no-extras", action="store_true",
+                   help="skip the batched (256-scene) and served (request stream) samples of the default line")
     p.add_argument("--e2e-contexts", type=int, default=3,
                    help="contexts taking alternate end-to-end steps (frames in flight)")
     return p.parse_args()
 
 
-def make_workload(name):
+def make_workload(name, args=None):
     from minirender_gb300 import workloads as W
     if name == "config1":
         st, sc = W.config1()
         desc = "uv-sphere 64x32 (3,968 tris), 640x480, point light, RGB8+depth"
     elif name == "config3":
-        st, sc = W.config3()
-        desc = "10M-triangle soup (1-4 px^2, 5% exact duplicates), 3840x2160, palette texture"
+        n = getattr(args, "triangles", None) or 10_000_000
+        w, h = (int(x) for x in (getattr(args, "size", None) or "3840x2160").split("x"))
+        st, sc = W.config3(n_tris=n, width=w, height=h)
+        desc = f"{n:,}-triangle soup (1-4 px^2, 5% exact duplicates), {w}x{h}, palette texture"
     else:
         st, sc = W.config2()
         desc = ("icosphere level 8 (1,310,720 tris) displaced by value noise, 1024^2 RGB8 "
@@ -180,12 +187,51 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def ncu_traffic(workload: str):
+def ncu_counts(workload: str):
+    """Per-kernel figures of one ncu capture of this workload (profiles/):
+    {kernel: {"dram_bytes": read + write bytes per launch, "warp_inst":
+    warp instructions per launch}}."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p):
         return {}
     with open(p) as f:
-        return json.load(f).get(workload, {})
+        d = json.load(f).get(workload, {})
+    return {k: v for k, v in d.items() if isinstance(v, dict)}
+
+
+# Sample workloads of the default line's batched and served objects, and the
+# fixed tunings they use (the autotuner's choice for the 256-scene batch on
+# GB300; the render server's default for the request stream).
+BATCH_SAMPLE_TUNING = {"tile_w": 64, "tile_h": 32, "threads": 256, "chunk": 64, "small_max": 64}
+SERVE_SAMPLE = {"rate": 5000.0, "requests": 300, "slots": 3, "max_batch": 16, "tuning": (16, 16, 64, 64, 64)}
+
+
+def extras(local, stream):
+    """The batched and served forms on short samples of their workloads, each
+    next to the plain one-frame-per-call path on the same frames."""
+    from minirender_gb300 import workloads as W
+    out = {}
+    items = W.config4(256)
+    m = batch_measure(local, stream, items, steps=3, warmup=3, tuning=BATCH_SAMPLE_TUNING, profile=False)
+    out["batched_config4"] = {
+        "value": round(m["value"], 2), "unit": UNIT, "scenes": len(items), "batches_timed": 3,
+        "ms_per_batch": round(m["total_s"] * 1e3 / 3, 4), "triangles_per_batch": m["T"],
+        "pixels_per_batch": m["P"], "tuning": BATCH_SAMPLE_TUNING,
+        "workload": "256 seeded scenes x 64 primitives, resolutions from {256^2, 512^2, 640x480, 1280x720}; "
+                    "one mr_render_batch per step (CUDA graph replay), 3 steps back to back",
+        "plain_one_frame_per_call": round(m["plain"], 2),
+        "speedup_vs_plain": round(m["value"] / m["plain"], 3)}
+    S = SERVE_SAMPLE
+    rows, plain = serve_measure(local, [S["rate"]], S["requests"], S["slots"], S["max_batch"], S["tuning"])
+    out["served_config5"] = {
+        "unit": UNIT, "requests_per_stream": S["requests"],
+        "workload": "Poisson request stream of triangle soups (log-uniform 1k-2M triangles, 128x128.."
+                    "3840x2160, 30 % re-renders of a resident mesh), 40 GB budget, RGB8 read back",
+        "server": {"slots": S["slots"], "max_batch": S["max_batch"], "tuning": list(S["tuning"])},
+        "at_rate": rows[0], "capacity": rows[1], "plain_at_rate": plain[0], "plain_capacity": plain[1],
+        "served_vs_plain_at_rate": round(rows[0]["frames_per_s"] / plain[0]["frames_per_s"], 3),
+        "served_vs_plain_capacity": round(rows[1]["frames_per_s"] / plain[1]["frames_per_s"], 3)}
+    return out
 
 
 _MESH_ARRAYS = ("vertices", "normals", "indices", "normalsI", "texcoords", "texcoordsI")
@@ -374,50 +420,41 @@ def batched_views(args, stream, flush, st, sc, views: int):
     return views * args.steps / (tot / 1e3), best
 
 
-def batch_arm(args, ws, rank, local):
-    """Config 4: `--scenes` independent scenes (seeded primitive hierarchies,
-    mixed resolutions) per step, rendered in one batched launch; compared with
-    the plain one-frame-per-call path on the same scenes."""
+def batch_measure(local, stream, items, steps, warmup, tuning=None, ws=1, profile=True):
+    """`steps` batches of `items` (one mr_render_batch each, CUDA graph
+    replay, K batches back to back between two CUDA events) and the same
+    scenes through the plain path, one mr_render per scene.  tuning: a dict
+    of TUNING_KEYS, or None for the autotuner."""
     import torch
-    from minirender_gb300 import abi, autotune, build
-    build.build()
-    from minirender_gb300 import workloads as W
+    from minirender_gb300 import abi, autotune
     from minirender_gb300.batch import BatchRenderer
     from minirender_gb300.renderer import Renderer
-    torch.cuda.set_device(local)
-    stream = torch.cuda.Stream()
-    torch.cuda.set_stream(stream)
-    items = W.config4(args.scenes)
     br = BatchRenderer(local)
     br.ctx.set_stream(stream.cuda_stream)
     br.outputs = abi.MR_OUT_RGB8 | abi.MR_OUT_DEPTH
     prep = br.prepare(items)
     T = sum(scene_tris(sc) for st, sc in items)
     P = sum(st.width * st.height for st, sc in items)
-    if args.tuning:
-        tun = [int(x) for x in args.tuning.split(",")]
-        if len(tun) == 3:
-            tun = [tun[0]] + tun
-        if len(tun) == 4:
-            tun.append(autotune.DEFAULT_SMALL_MAX)
-        best = {"tile_w": tun[0], "tile_h": tun[1], "threads": tun[2], "chunk": tun[3], "small_max": tun[4],
-                "table": None}
+    if tuning is not None:
+        best = dict(tuning, table=None)
         autotune.apply(br.ctx, best)
     else:
         best = autotune.tune(br.ctx, prep, autotune.batch_class(len(items), T, P))
     br.ctx.set_batch_graphs(True)
-    for _ in range(max(3, args.warmup)):
+    for _ in range(max(3, warmup)):
         br.ctx.render_batch(*prep, br.outputs)
     br.ctx.batch_stats()
-    br.ctx.set_profiling(True)
-    br.ctx.set_batch_graphs(False)  # stage events need a launch outside the graph
-    br.ctx.render_batch(*prep, br.outputs)
-    s = br.ctx.batch_stats()
-    stage = [round(float(x), 4) for x in s.stage_ms[:3]]
-    br.ctx.set_profiling(False)
-    br.ctx.set_batch_graphs(True)
-    br.ctx.render_batch(*prep, br.outputs)
-    br.ctx.batch_stats()
+    stage = [None, None, None]
+    if profile:
+        br.ctx.set_profiling(True)
+        br.ctx.set_batch_graphs(False)  # stage events need a launch outside the graph
+        br.ctx.render_batch(*prep, br.outputs)
+        s = br.ctx.batch_stats()
+        stage = [round(float(x), 4) for x in s.stage_ms[:3]]
+        br.ctx.set_profiling(False)
+        br.ctx.set_batch_graphs(True)
+        br.ctx.render_batch(*prep, br.outputs)
+        br.ctx.batch_stats()
     clocks = Clocks(local)
     barrier(ws)
     torch.cuda.synchronize()
@@ -429,16 +466,16 @@ def batch_arm(args, ws, rank, local):
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         br.ctx.render_batch(*prep, br.outputs)
     e1.record(stream)
     e1.synchronize()
     clk = clocks.stop()
     total_s = max_over_ranks(e0.elapsed_time(e1) / 1e3, ws)
-    value = len(items) * args.steps * ws / total_s
+    value = len(items) * steps * ws / total_s
     # one batch at a time, waiting for each (host staging not overlapped)
     t0 = time.perf_counter()
-    for _ in range(args.steps):
+    for _ in range(steps):
         br.ctx.render_batch(*prep, br.outputs)
         br.ctx.synchronize()
     wall = time.perf_counter() - t0
@@ -456,12 +493,12 @@ def batch_arm(args, ws, rank, local):
     r.ctx.synchronize()
     # the same scenes one mr_render each, back to back between two events
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(steps):
         for f, rs, n in per:
             r.ctx.render(f, rs, n, r.outputs)
     e1.record(stream)
     e1.synchronize()
-    plain = len(items) * args.steps / (e0.elapsed_time(e1) / 1e3)
+    plain = len(items) * steps / (e0.elapsed_time(e1) / 1e3)
     t0 = time.perf_counter()
     for f, rs, n in per:
         r.ctx.render(f, rs, n, r.outputs)
@@ -469,9 +506,36 @@ def batch_arm(args, ws, rank, local):
     plain_wall = len(items) / (time.perf_counter() - t0)
     r.close()
     br.close()
+    return {"value": value, "total_s": total_s, "T": T, "P": P, "best": best, "stage": stage, "clocks": clk,
+            "wall_value": len(items) * steps / wall, "plain": plain, "plain_wall": plain_wall}
+
+
+def batch_arm(args, ws, rank, local):
+    """Config 4: `--scenes` independent scenes (seeded primitive hierarchies,
+    mixed resolutions) per step, rendered in one batched launch; compared with
+    the plain one-frame-per-call path on the same scenes."""
+    import torch
+    from minirender_gb300 import autotune, build
+    build.build()
+    from minirender_gb300 import workloads as W
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    items = W.config4(args.scenes)
+    tuning = None
+    if args.tuning:
+        tun = [int(x) for x in args.tuning.split(",")]
+        if len(tun) == 3:
+            tun = [tun[0]] + tun
+        if len(tun) == 4:
+            tun.append(autotune.DEFAULT_SMALL_MAX)
+        tuning = dict(zip(TUNING_KEYS, tun))
+    m = batch_measure(local, stream, items, args.steps, args.warmup, tuning, ws)
+    best, P, T = m["best"], m["P"], m["T"]
+    value = m["value"]
     return {
         "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": ws, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": round(total_s * 1e3 / args.steps, 4),
+        "warmup": args.warmup, "ms_per_step": round(m["total_s"] * 1e3 / args.steps, 4),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded generator)",
         "config": {"workload": f"{len(items)} scenes x 64 primitives (cube/sphere/cylinder, 8-64 segments), "
@@ -483,37 +547,34 @@ def batch_arm(args, ws, rank, local):
                    "timing": "K batches back to back between two CUDA events (host staging overlapped)",
                    "tuning": {k: best[k] for k in TUNING_KEYS}},
         "mtri_per_s": round(value * T / len(items) / 1e6, 2),
-        "wall_value_one_batch_at_a_time": round(len(items) * args.steps / wall, 2),
-        "plain_one_frame_per_call": {"value": round(plain, 2), "wall_value": round(plain_wall, 2),
+        "wall_value_one_batch_at_a_time": round(m["wall_value"], 2),
+        "plain_one_frame_per_call": {"value": round(m["plain"], 2), "wall_value": round(m["plain_wall"], 2),
                                      "unit": UNIT},
-        "speedup_vs_plain": round(value / plain, 3),
-        "stage_ms": {"vertex": stage[0], "setup": stage[1], "fused_bin_raster_shade": stage[2]},
+        "speedup_vs_plain": round(value / m["plain"], 3),
+        "stage_ms": {"vertex": m["stage"][0], "setup": m["stage"][1], "fused_bin_raster_shade": m["stage"][2]},
         "autotune_table": best.get("table"),
-        "gpu_launches": 3 * args.steps, "clocks": clk,
+        "gpu_launches": 3 * args.steps, "clocks": m["clocks"],
     }
 
 
-
-def serve_arm(args, ws, rank, local):
-    """Config 5: Poisson request streams at swept rates through the render
-    server (continuous batching, resident meshes, 40 GB budget) and the same
-    sequence through the plain one-frame-per-call path."""
+def serve_measure(local, rates, n_requests, slots, max_batch, tuning, pool=None, plain_rates=None):
+    """Poisson request streams (one per rate in `rates`, then one with every
+    request queued at t = 0) through the render server, and the plain path
+    (one mr_render + read per request) on the streams of `plain_rates`
+    (default: the highest rate and the all-queued one)."""
     import torch
-    from minirender_gb300 import abi, build
-    build.build()
-    from minirender_gb300 import capi
+    from minirender_gb300 import abi, capi
     from minirender_gb300 import workloads as W
-    from minirender_gb300.scene import Scene
     from minirender_gb300.server import RenderServer
-    torch.cuda.set_device(local)
-    pool = W.config5_pool()
-    # the asset store lives in page-locked host memory (uploads are DMA, the
-    # same for the server and the plain path)
-    for m in pool:
-        _pin_mesh(m)
+    if pool is None:
+        pool = W.config5_pool()
+        # the asset store lives in page-locked host memory (uploads are DMA,
+        # the same for the server and the plain path)
+        for m in pool:
+            _pin_mesh(m)
     ctx = capi.Context(local)
-    tw, th, tthreads, tchunk, tsmall = (int(x) for x in args.serve_tuning.split(","))
-    srv = RenderServer(ctx, budget_bytes=40 << 30, slots=args.serve_slots, max_batch=args.serve_max_batch, tile=tw,
+    tw, th, tthreads, tchunk, tsmall = tuning
+    srv = RenderServer(ctx, budget_bytes=40 << 30, slots=slots, max_batch=max_batch, tile=tw,
                        tile_h=th, threads=tthreads, chunk=tchunk, small_max=tsmall)
     maxpx = 3840 * 2160
     ring = [torch.empty(maxpx * 3, dtype=torch.uint8).pin_memory().numpy() for _ in range(96)]
@@ -548,10 +609,9 @@ def serve_arm(args, ws, rank, local):
     stream(W.config5_requests(pool, 64, 1000.0, seed=1, key_base=next(keys)))
     stream(W.config5_requests(pool, 384, math.inf, seed=2, key_base=next(keys)))
     rows = []
-    rates = [float(x) for x in args.rates.split(",")]
     # capacity: every request queued at t = 0 (rate "inf")
-    for rate in rates + [math.inf]:
-        reqs = W.config5_requests(pool, args.requests, rate, seed=_rate_seed(rate), key_base=next(keys))
+    for rate in list(rates) + [math.inf]:
+        reqs = W.config5_requests(pool, n_requests, rate, seed=_rate_seed(rate), key_base=next(keys))
         srv.reset_stats()
         wall = stream(reqs)
         s = srv.stats()
@@ -560,15 +620,27 @@ def serve_arm(args, ws, rank, local):
                      "max_ms": round(s["max_us"] / 1e3, 3), "mean_batch": round(s["mean_batch"], 2),
                      "requests": int(s["completed"])})
     srv.close()
-    # plain path on the highest-rate sequence and on the capacity sequence: one
-    # mr_render + read per request, new meshes uploaded with mr_mesh_upload,
-    # resident meshes kept (LRU by key)
-    from minirender_gb300.renderer import Renderer
-    plain_rows = [plain_stream(args, pool, ring, local, rate) for rate in (rates[-1], math.inf)]
     ctx.close()
+    plain_rates = plain_rates or (rates[-1], math.inf)
+    plain_rows = [plain_stream(n_requests, pool, ring, local, rate) for rate in plain_rates]
+    return rows, plain_rows
+
+
+def serve_arm(args, ws, rank, local):
+    """Config 5: Poisson request streams at swept rates through the render
+    server (continuous batching, resident meshes, 40 GB budget) and the same
+    sequence through the plain one-frame-per-call path."""
+    import torch
+    from minirender_gb300 import build
+    build.build()
+    torch.cuda.set_device(local)
+    tuning = tuple(int(x) for x in args.serve_tuning.split(","))
+    rates = [float(x) for x in args.rates.split(",")]
+    rows, plain_rows = serve_measure(local, rates, args.requests, args.serve_slots, args.serve_max_batch, tuning)
     served = rows[:-1]
     cap = rows[-1]
     best = max(served, key=lambda x: x["frames_per_s"])
+    tw, th, tthreads, tchunk, tsmall = tuning
     return {
         "metric": METRIC, "value": best["frames_per_s"], "unit": UNIT, "n_gpus": ws,
         "steps": args.requests, "warmup": 64, "ms_per_step": round(1e3 / best["frames_per_s"], 4),
@@ -603,13 +675,13 @@ def _rate_label(rate: float):
     return rate if math.isfinite(rate) else "all queued at t=0"
 
 
-def plain_stream(args, pool, ring, local, rate):
+def plain_stream(n_requests, pool, ring, local, rate):
     """The request sequence of `rate` through the plain path, one
     mr_render + synchronous read per request (arrival times honoured)."""
     from minirender_gb300 import abi
     from minirender_gb300 import workloads as W
     from minirender_gb300.renderer import Renderer
-    reqs = W.config5_requests(pool, args.requests, rate, seed=_rate_seed(rate))
+    reqs = W.config5_requests(pool, n_requests, rate, seed=_rate_seed(rate))
     r = Renderer(local)
     r.outputs = abi.MR_OUT_RGB8
     resident = {}
@@ -659,7 +731,7 @@ def gpu_arm(args, ws, rank, local):
     from minirender_gb300.renderer import Renderer
 
     torch.cuda.set_device(local)
-    st, sc, desc = make_workload(args.workload)
+    st, sc, desc = make_workload(args.workload, args)
     V, T, mesh_bytes, tex_bytes = scene_sizes(sc)
     P = st.width * st.height
     r = Renderer(local)
@@ -739,7 +811,16 @@ def gpu_arm(args, ws, rank, local):
     }
     peak, peak_kind = peaks()
     achieved = alg[name] / (stage_ms[dom] / 1e3) / 1e9
-    traffic = ncu_traffic(args.workload).get(KERNELS[name])
+    counts = ncu_counts(args.workload).get(KERNELS[name], {})
+    traffic = counts.get("dram_bytes")
+    # instruction-issue ceiling: warp instructions of one launch (ncu) over
+    # what the SMs' four schedulers can issue in the kernel's event time at
+    # the median SM clock of the timed region
+    n_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz")
+    issue_frac = None
+    if counts.get("warp_inst") and mhz:
+        issue_frac = counts["warp_inst"] / (n_sms * 4 * mhz * 1e6 * stage_ms[dom] / 1e3)
     frame_bytes = (32 * V if vertex_pass else 12 * V) + 36 * T + 16 * P + 7 * P + 3 * tex_px
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": ws,
@@ -761,7 +842,9 @@ def gpu_arm(args, ws, rank, local):
         "roofline": {"bound": "hbm", "kernel": KERNELS[name], "achieved": round(achieved, 2),
                      "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "peak_source": peak_kind, "traffic": traffic,
-                     "algorithmic_bytes": int(alg[name]), "kernel_ms": round(float(stage_ms[dom]), 5)},
+                     "algorithmic_bytes": int(alg[name]), "kernel_ms": round(float(stage_ms[dom]), 5),
+                     "issue_frac": None if issue_frac is None else round(issue_frac, 4),
+                     "warp_inst": counts.get("warp_inst"), "sms": n_sms},
         "stage_ms": {k: round(float(v), 5) for k, v in zip(STAGES, stage_ms)},
         "frame_roofline": {"algorithmic_bytes": int(frame_bytes),
                            "achieved_gbs": round(frame_bytes / (total_s / args.steps * ws) / 1e9, 2),
@@ -778,6 +861,8 @@ def gpu_arm(args, ws, rank, local):
         out["batched"] = {"value": round(bv, 3), "unit": UNIT, "views_per_launch": args.views,
                           "speedup_vs_plain": round(bv / value, 3),
                           "tuning": {k: best[k] for k in TUNING_KEYS}}
+    if args.workload == "config2" and not args.no_extras:
+        out.update(extras(local, stream))
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         n_threads = os.cpu_count() or 1
         frames = 2 * n_threads
@@ -795,7 +880,7 @@ def gpu_arm(args, ws, rank, local):
 def reference_arm(args, ws, rank):
     if rank != 0:
         return None
-    st, sc, desc = make_workload(args.workload)
+    st, sc, desc = make_workload(args.workload, args)
     V, T, _, _ = scene_sizes(sc)
     n_threads = os.cpu_count() or 1
     for _ in range(max(0, args.warmup)):
