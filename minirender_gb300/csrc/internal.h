@@ -55,12 +55,16 @@ template <typename T>
 struct DevBuf {
   T* p = nullptr;
   size_t cap = 0;  // elements
+  // Grows to at least 1.5x the old capacity: a stream of frames or batches
+  // of varying sizes then reallocates O(log) times, not at every new
+  // maximum (each cudaFree waits for the whole device).
   cudaError_t ensure(size_t n) {
     if (n <= cap && p) return cudaSuccess;
+    const size_t grown = cap + cap / 2;
     if (p) cudaFree(p);
     p = nullptr;
     cap = 0;
-    size_t want = std::max<size_t>(n, 1);
+    size_t want = std::max<size_t>(std::max<size_t>(n, grown), 1);
     cudaError_t e = cudaMalloc(&p, want * sizeof(T));
     if (e == cudaSuccess) cap = want;
     return e;
