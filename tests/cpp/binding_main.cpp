@@ -17,6 +17,11 @@
 //   paintmesh MESH HAS_MATERIAL d0..e2 SHININESS TEXTURE t0..t15
 //   material d0..e2 SHININESS TEXTURE            (setMaterial)
 //   triangle WORLD x y z nx ny nz u v x y z nx ny nz u v x y z nx ny nz u v
+//   scale NODE F   scales the node's mesh vertices by F in place, then
+//                  GpuRenderer::meshChanged (same arrays, new contents)
+//   grow NODE T    appends one triangle (a copy of triangle T, pushed 0.5
+//                  along +z) to the node's mesh: the arrays are reallocated
+//                  and longer, which the binding must notice
 //   out PREFIX   -> PREFIX.image/.depth/.rgb8/.ids/.range[/.normals]
 // Exit status 3 with the message on stdout when the binding throws GpuError.
 #include <stdio.h>
@@ -119,7 +124,7 @@ int run(const char* scene_file) {
   std::vector<asl::Shared<SceneNode>> nodes;
   std::vector<asl::Shared<TriMesh>> painted;  // paintMesh meshes stay alive until exit
   asl::Shared<Scene> scene;
-  bool save_normals = false;
+  bool save_normals = false, scene_set = false;
   std::string line;
   while (std::getline(file, line)) {
     std::istringstream in(line);
@@ -192,7 +197,8 @@ int run(const char* scene_file) {
     } else if (cmd == "ambient") {
       in >> scene->ambientLight;
     } else if (cmd == "render") {
-      r.setScene(scene);
+      if (!scene_set) r.setScene(scene);  // once: setScene forgets the mesh cache
+      scene_set = true;
       r.render();
     } else if (cmd == "clear") {
       r.clear();
@@ -218,6 +224,32 @@ int run(const char* scene_file) {
         x.uv = asl::Vec2(u, w);
       }
       r.paintTriangle(v[0], v[1], v[2], world != 0);
+    } else if (cmd == "scale") {
+      int k;
+      float f;
+      in >> k >> f;
+      TriMesh* m = dynamic_cast<TriMesh*>(nodes[k].operator->());
+      if (!m) throw std::runtime_error("scale: not a mesh node");
+      for (int i = 0; i < m->vertices.length(); i++)
+        m->vertices[i] = asl::Vec3(m->vertices[i].x * f, m->vertices[i].y * f, m->vertices[i].z * f);
+      r.meshChanged(m);
+    } else if (cmd == "grow") {
+      int k, t;
+      in >> k >> t;
+      TriMesh* m = dynamic_cast<TriMesh*>(nodes[k].operator->());
+      if (!m) throw std::runtime_error("grow: not a mesh node");
+      const int nv = m->vertices.length(), nn = m->normals.length(), nt = m->texcoords.length();
+      for (int c = 0; c < 3; c++) {
+        const asl::Vec3 v = m->vertices[m->indices[3 * t + c]];
+        m->vertices << asl::Vec3(v.x, v.y, v.z + 0.5f);
+        m->normals << m->normals[m->normalsI[3 * t + c]];
+        if (nt && m->texcoordsI.length()) m->texcoords << m->texcoords[m->texcoordsI[3 * t + c]];
+      }
+      for (int c = 0; c < 3; c++) {
+        m->indices << nv + c;
+        m->normalsI << nn + c;
+        if (nt && m->texcoordsI.length()) m->texcoordsI << nt + c;
+      }
     } else if (cmd == "out") {
       std::string prefix;
       in >> prefix;

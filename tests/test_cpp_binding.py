@@ -252,3 +252,49 @@ def test_binding_loaded_models(product_lib, tmp_path, name):
     stats = compare(got, ref, f"cpp_binding_{name}")
     assert_parity(stats)
     assert stats["covered"] > 100
+
+
+@pytest.mark.gpu
+def test_binding_notices_mesh_edits(product_lib, tmp_path):
+    """The binding's mesh cache: a mesh scaled in place and announced with
+    meshChanged(), then a mesh whose arrays grew (reallocated, longer), are
+    each sent again -- every frame equals the oracle's render of the edited
+    scene, and each edit changes the picture."""
+    from minirender_gb300.scene import Scene, TriMesh
+    st, sc0 = W.config1(160, 120)
+    m0 = sc0.children[0]
+    v0, n0, i0, ni0 = m0.vertices.copy(), m0.normals.copy(), m0.indices.copy(), m0.normalsI.copy()
+
+    def scene_of(v, n, i, ni):
+        sc = Scene()
+        sc.add(TriMesh(v, n, i, normalsI=ni, material=m0.material))
+        return sc
+
+    exe = build_driver(str(tmp_path))
+    w = SceneWriter(str(tmp_path))
+    w.state(st)
+    w.scene(scene_of(v0, n0, i0, ni0))
+    # the triangle facing the camera most directly (largest centroid z)
+    t = int(np.argmax(v0[i0.reshape(-1, 3)].mean(axis=1)[:, 2]))
+    w.lines += ["render", f"out {tmp_path}/a", "scale 1 0.75", "render", f"out {tmp_path}/b",
+                f"grow 1 {t}", "render", f"out {tmp_path}/c"]
+    r = run_driver(exe, w.write())
+    assert r.returncode == 0, r.stdout + r.stderr
+    # the same edits on the Python side, in float32 as the driver makes them
+    v1 = v0 * np.float32(0.75)
+    corner = v1[i0[3 * t:3 * t + 3]].copy()
+    corner[:, 2] = corner[:, 2] + np.float32(0.5)
+    nv, nn = v1.shape[0], n0.shape[0]
+    v2 = np.concatenate([v1, corner])
+    n2 = np.concatenate([n0, n0[ni0[3 * t:3 * t + 3]]])
+    i2 = np.concatenate([i0, np.arange(nv, nv + 3, dtype=np.int32)])
+    ni2 = np.concatenate([ni0, np.arange(nn, nn + 3, dtype=np.int32)])
+    previous = None
+    for tag, sc in (("a", scene_of(v0, n0, i0, ni0)), ("b", scene_of(v1, n0, i0, ni0)),
+                    ("c", scene_of(v2, n2, i2, ni2))):
+        got = read_outputs(f"{tmp_path}/{tag}", st)
+        stats = compare(got, O.render(st, sc), f"cpp_binding_edit_{tag}")
+        assert_parity(stats)
+        if previous is not None:
+            assert not np.array_equal(got["ids"], previous), f"frame {tag} did not change"
+        previous = got["ids"]
