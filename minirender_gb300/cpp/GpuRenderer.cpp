@@ -1,6 +1,10 @@
 // GpuRenderer: minirender's Renderer on the GB300 path (see GpuRenderer.h).
 #include "GpuRenderer.h"
 
+#include <string.h>
+
+#include <set>
+
 namespace minirender {
 
 namespace {
@@ -8,6 +12,13 @@ namespace {
 void rowMajor(const asl::Matrix4& m, float* o) {
   for (int i = 0; i < 4; i++)
     for (int j = 0; j < 4; j++) o[4 * i + j] = m(i, j);
+}
+
+bool sameMatrix(const asl::Matrix4& a, const asl::Matrix4& b) {
+  float x[16], y[16];
+  rowMajor(a, x);
+  rowMajor(b, y);
+  return memcmp(x, y, sizeof(x)) == 0;
 }
 
 template <class T>
@@ -82,6 +93,7 @@ void GpuRenderer::clear() {
     if (r.handle >= 0) mr_mesh_free(_ctx, r.handle);
   _runs.clear();
   _drawn = asl::Shared<Scene>();
+  _haveFrameView = false;
   _rendered = false;
   _have = false;
 }
@@ -95,6 +107,8 @@ void GpuRenderer::render() {
   _scene->collectShapes(list, asl::Matrix4::identity());
   clear();
   _drawn = _scene;
+  _frameView = _view;  // the light is placed with it (src/Renderer.cpp:317-320)
+  _haveFrameView = true;
   for (int i = 0; i < list.length(); i++) {
     Item it;
     it.mesh = list[i].mesh;
@@ -110,9 +124,25 @@ void GpuRenderer::render() {
 // the current view and `transform`, in the mesh's material or the default.
 void GpuRenderer::paintMesh(TriMesh* mesh, const asl::Matrix4& transform) {
   if (!mesh) throw GpuError(MR_E_INVALID, "paintMesh: null mesh");
+  if (!_haveFrameView) {
+    _frameView = _view;
+    _haveFrameView = true;
+  }
   Item it;
   it.mesh = mesh;
   it.transform = transform;
+  if (!sameMatrix(_view, _frameView)) {
+    // the view changed since the frame's light was placed: the modelview
+    // of this call, _view * transform (src/Renderer.cpp:337), composed as
+    // the library composes it
+    float v[16], t[16], m[16];
+    rowMajor(_view, v);
+    rowMajor(transform, t);
+    mr_mat4_mul(v, t, m);
+    it.transform = asl::Matrix4(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], m[11], m[12],
+                                m[13], m[14], m[15]);
+    it.flags = MR_RS_MODELVIEW;
+  }
   it.material = mesh->material ? mesh->material : _defmaterial;
   _material = it.material;
   _items.push_back(it);
@@ -126,6 +156,10 @@ void GpuRenderer::paintMesh(TriMesh* mesh, const asl::Matrix4& transform) {
 // one mesh whose modelview is the identity (MR_RS_MODELVIEW).
 void GpuRenderer::paintTriangle(const Vertex& a, const Vertex& b, const Vertex& c, bool world) {
   const int32_t flags = MR_RS_MODELVIEW | (world ? 0 : MR_RS_NO_CLIP);
+  if (!_haveFrameView) {
+    _frameView = _view;
+    _haveFrameView = true;
+  }
   asl::Shared<Material> mat = _material ? _material : _defmaterial;
   if (_items.empty() || _items.back().run < 0 || _items.back().flags != flags ||
       _items.back().material.operator->() != mat.operator->()) {
@@ -247,7 +281,7 @@ mr_frame GpuRenderer::frame() const {
   f.width = _w;
   f.height = _h;
   rowMajor(_projection, f.projection);
-  rowMajor(_view, f.view);
+  rowMajor(_haveFrameView ? _frameView : _view, f.view);
   f.light[0] = _light.x;
   f.light[1] = _light.y;
   f.light[2] = _light.z;
@@ -280,6 +314,33 @@ void GpuRenderer::flush() {
         "render");
   _rendered = true;
   _have = false;
+  prune();
+}
+
+// Frees the cached meshes and textures the frame just drawn does not use.
+void GpuRenderer::prune() {
+  std::set<TriMesh*> meshes;
+  std::set<Material*> materials;
+  for (const Item& it : _items) {
+    if (it.mesh) meshes.insert(it.mesh);
+    materials.insert(it.material.operator->());
+  }
+  for (auto i = _meshes.begin(); i != _meshes.end();) {
+    if (meshes.count(i->first)) {
+      ++i;
+      continue;
+    }
+    if (i->second.handle >= 0) mr_mesh_free(_ctx, i->second.handle);
+    i = _meshes.erase(i);
+  }
+  for (auto i = _textures.begin(); i != _textures.end();) {
+    if (materials.count(i->first)) {
+      ++i;
+      continue;
+    }
+    if (i->second.handle >= 0) mr_texture_free(_ctx, i->second.handle);
+    i = _textures.erase(i);
+  }
 }
 
 void GpuRenderer::read() {

@@ -25,7 +25,17 @@
 //    is announced with textureChanged().
 //  * paintMesh / paintTriangle after render() or clear() are recorded and
 //    rendered with the frame, in call order, when an image is next read: the
-//    same pixels as painting them one after the other.
+//    same pixels as painting them one after the other.  As in the
+//    reference, paintMesh uses the view current at the call, and the light
+//    is placed with the view of the last render() (or, with none since
+//    clear(), of the first paint).  The other state (size, projection,
+//    light, lighting, texturing, normals, background) is the frame's: the
+//    state when the image is read.
+//  * The caches hold the meshes and textures of the frame last drawn:
+//    entries the next frame does not use are freed.  A TriMesh or Material
+//    destroyed and replaced by another at the same address with arrays of
+//    the same addresses and lengths is taken for the old one unless
+//    meshChanged() / textureChanged() says otherwise.
 //  * Beyond the reference: getImageRGB8() (savePPM's bytes, src/io.cpp:
 //    358-362, computed on the device) and getTriangleIds().
 #ifndef MINIRENDER_GPU_RENDERER_H
@@ -117,6 +127,7 @@ class GpuRenderer {
   };
 
   void check(int status, const char* what) const;
+  void prune();
   int32_t meshHandle(TriMesh* m);
   int32_t textureHandle(const asl::Shared<Material>& mat);
   int32_t runHandle(TriangleRun& r);
@@ -127,6 +138,8 @@ class GpuRenderer {
   mr_ctx* _ctx = nullptr;
   int _w = 0, _h = 0;
   asl::Matrix4 _projection, _view;
+  asl::Matrix4 _frameView;      // the view that places the frame's light
+  bool _haveFrameView = false;
   asl::Vec3 _light, _bgcolor;
   bool _lightIsPoint = false, _lighting = true, _texturing = true, _saveNormals = false;
   asl::Shared<Scene> _scene;

@@ -11,9 +11,12 @@ results back.
 reference's do: after ``clear()`` (or ``render()``) the paints are recorded
 and the next getter renders the scene's renderables and the paints, in call
 order, as one frame -- the same pixels as painting them one after the other
-(later fragments win only with a strictly smaller depth).  Frame-wide state
-(size, projection, light, lighting, texturing, background, normals) is the
-state when the frame is read.
+(later fragments win only with a strictly smaller depth).  As in the
+reference, ``paintMesh`` uses the view current at the call and the light is
+placed with the view of the last ``render()`` (or, with none since
+``clear()``, of the first paint).  The other state (size, projection, light,
+lighting, texturing, background, normals) is the frame's: the state when the
+frame is read.
 """
 from __future__ import annotations
 
@@ -38,6 +41,7 @@ class Renderer:
         self._rendered = False
         self._base = None                      # (renderables, count) of the last render()
         self._paints: list = []                # paintMesh / paintTriangle since then
+        self._frame_view = None                # the view that places the frame's light
         self._dirty = False
         self.outputs = abi.MR_OUT_DEFAULT | abi.MR_OUT_RGB_F32
 
@@ -86,7 +90,16 @@ class Renderer:
         self._rendered = False
         self._base = None
         self._paints = []
+        self._frame_view = None
         self._dirty = False
+
+    def _paint_view(self) -> np.ndarray:
+        """The view at a paint call; the first paint after clear() fixes the
+        frame's view."""
+        view = np.asarray(self.state.view, np.float32).reshape(4, 4)
+        if self._frame_view is None:
+            self._frame_view = view.copy()
+        return view
 
     def paintMesh(self, mesh: sc.TriMesh, transform=None):
         """Renderer::paintMesh (src/Renderer.cpp:334-381): the mesh with the
@@ -95,7 +108,15 @@ class Renderer:
         mat = mesh.material if mesh.material is not None else sc.Material()
         self._material = mat
         xf = sc.identity() if transform is None else transform
-        self._paints.append(sc.Paint(mesh, xf, mat, 0))
+        view = self._paint_view()
+        if view.tobytes() == self._frame_view.tobytes():
+            self._paints.append(sc.Paint(mesh, xf, mat, 0))
+        else:
+            # the view changed since the frame's light was placed: this
+            # call's modelview, _view * transform (src/Renderer.cpp:337),
+            # composed as the library composes it
+            mv = capi.mat4_mul(view, np.asarray(xf, np.float32).reshape(4, 4))
+            self._paints.append(sc.Paint(mesh, mv, mat, abi.MR_RS_MODELVIEW))
         self._dirty = True
 
     def paintTriangle(self, a: sc.Vertex, b: sc.Vertex, c: sc.Vertex, world: bool = True):
@@ -103,6 +124,7 @@ class Renderer:
         of view-space vertices in the current material; world=False skips the
         near-plane clipping."""
         mat = self._material if self._material is not None else sc.Material()
+        self._paint_view()
         flags = abi.MR_RS_MODELVIEW | (0 if world else abi.MR_RS_NO_CLIP)
         last = self._paints[-1] if self._paints else None
         if last is not None and last.flags == flags and last.material is mat and getattr(last, "run", False):
@@ -160,6 +182,7 @@ class Renderer:
         self._rendered = True
         self._base = (rs, n)
         self._paints = []
+        self._frame_view = np.asarray(self.state.view, np.float32).reshape(4, 4).copy()
         self._dirty = False
 
     def _flush_paints(self):
@@ -172,7 +195,10 @@ class Renderer:
             rs[i] = base_rs[i]
         for j in range(len(self._paints)):
             rs[base_n + j] = prs[j]
-        self.ctx.render(self.state.to_c(), rs, n, self.outputs)
+        frame = self.state.to_c()
+        if self._frame_view is not None:
+            frame.view[:] = [float(x) for x in self._frame_view.reshape(16)]
+        self.ctx.render(frame, rs, n, self.outputs)
         self._rendered = True
         self._dirty = False
         self._out = None

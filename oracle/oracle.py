@@ -342,7 +342,7 @@ def ref_paint(state: FrameState, paints, clear: bool = False) -> dict:
     """The reference Renderer itself: render() of an empty scene (the state
     paintMesh uses), clear() if asked, then the paints in order -- paintMesh
     for a scene.Paint without MR_RS_MODELVIEW, setMaterial + paintTriangle
-    per triangle of a paintTriangle run."""
+    per triangle of a paintTriangle run, setView(m) for an item ("view", m)."""
     L = ref_lib()
     if L is None:
         raise RuntimeError("reference build unavailable")
@@ -356,6 +356,10 @@ def ref_paint(state: FrameState, paints, clear: bool = False) -> dict:
         return tex_ix[id(t)]
 
     for p in paints:
+        if isinstance(p, tuple) and p[0] == "view":
+            kind.append(2); mesh.append(-1); xf.append(np.asarray(p[1], np.float32).reshape(4, 4))
+            mats.append(abi.mr_material()); world.append(1); tri.append(np.zeros(24, np.float32))
+            continue
         m = abi.mr_material()
         tex = p.material.texture
         sc._fill_material(m, p.material, texture_index(tex) if tex is not None else -1)

@@ -329,7 +329,8 @@ static Shared<Material> make_material(const mr_material& mm, const RefTexture* t
 // direction, ambient and near plane paintMesh uses), optionally clear(),
 // then n_ops paints in order: kind 0 = paintMesh(meshes[mesh[i]] with
 // material[i], transform[16 i..]), kind 1 = setMaterial(material[i]) and
-// paintTriangle of tri[24 i..] (3 x position, normal, uv) with world[i].
+// paintTriangle of tri[24 i..] (3 x position, normal, uv) with world[i],
+// kind 2 = setView(transform[16 i..]) for the paints after it.
 int ref_paint(const mr_frame* f, const mr_mesh_desc* meshes, int32_t n_meshes, const RefTexture* tex,
               int32_t n_tex, int do_clear, int32_t n_ops, const int32_t* kind, const int32_t* mesh,
               const float* transform, const mr_material* material, const float* tri, const int32_t* world,
@@ -349,6 +350,10 @@ int ref_paint(const mr_frame* f, const mr_mesh_desc* meshes, int32_t n_meshes, c
   if (do_clear) r.clear();
   std::vector<Shared<TriMesh>> keep;
   for (int32_t i = 0; i < n_ops; i++) {
+    if (kind[i] == 2) {
+      r.setView(to_m4(transform + 16 * i));
+      continue;
+    }
     Shared<Material> mat = make_material(material[i], tex, n_tex);
     if (kind[i] == 0) {
       if (mesh[i] < 0 || mesh[i] >= n_meshes) return MR_E_HANDLE;

@@ -5,6 +5,7 @@ triangles, texture wrap-around, orthographic depth below zero, large
 triangles spanning many tiles, lighting variants."""
 import numpy as np
 
+from minirender_gb300 import abi
 from minirender_gb300 import projection as pj
 from minirender_gb300.frame import FrameState
 from minirender_gb300.scene import Material, Scene, SceneNode, TriMesh
@@ -231,6 +232,28 @@ def paint_sequence(w=160, h=120):
     paints.append(q)
     paints.append(Paint(sphere, t1, Material(diffuse=(0.1, 0.1, 0.9))))
     return st, paints
+
+
+def view_change_paints(w=160, h=120):
+    """paintMesh before and after setView, with a paintTriangle run between
+    (src/Renderer.cpp:163-381: paintMesh takes the view current at the call,
+    the light stays where render() placed it, view-space triangles ignore
+    the view).  Returns (state, calls, paints): `calls` as the reference
+    receives them (scene.Paint records and ("view", m) items), `paints` the
+    same frame as one paint list -- the paints after the view change carry
+    their modelview (view x transform, MR_RS_MODELVIEW)."""
+    from minirender_gb300.scene import Paint
+    st, seq = paint_sequence(w, h)
+    sphere_paint, quad_paint, run = seq[0], seq[1], seq[2]
+    v2 = pj.mat_mul(pj.translate(-0.4, 0.3, -4.5), pj.rotate_y(0.5))
+    t3 = pj.mat_mul(pj.translate(0.9, -0.5, 0.3), pj.scale(0.5))
+    last = Paint(sphere_paint.mesh, t3, Material(diffuse=(0.9, 0.2, 0.2), specular=(1, 1, 1), shininess=16))
+    calls = [sphere_paint, ("view", v2), quad_paint, run, last]
+    paints = [sphere_paint,
+              Paint(quad_paint.mesh, pj.mat_mul(v2, quad_paint.transform), quad_paint.material, abi.MR_RS_MODELVIEW),
+              run,
+              Paint(last.mesh, pj.mat_mul(v2, last.transform), last.material, abi.MR_RS_MODELVIEW)]
+    return st, calls, paints
 
 
 def random_scene(seed: int):

@@ -119,6 +119,9 @@ class SceneWriter:
 
     def paints(self, paints):
         for p in paints:
+            if isinstance(p, tuple):  # ("view", m): setView
+                self.lines.append(f"view {_floats(list(np.asarray(p[1], np.float32).reshape(16)))}")
+                continue
             tex = self.texture(p.material.texture) if p.material.texture is not None else -1
             if p.flags & abi.MR_RS_MODELVIEW:
                 world = 0 if p.flags & abi.MR_RS_NO_CLIP else 1
@@ -185,7 +188,9 @@ def _cases():
         yield f"random_{seed}", st, sc
     st, sc = W.config1(160, 120)
     _, paints = E.paint_sequence(160, 120)
-    yield "render_then_paints", st, (sc, paints)
+    yield "render_then_paints", st, (sc, paints, paints)
+    st, calls, paints = E.view_change_paints(160, 120)
+    yield "paints_after_view_change", st, (W.config1(160, 120)[1], calls, paints)
 
 
 def _fix(case):
@@ -203,10 +208,10 @@ def test_binding_matches_oracle(product_lib, tmp_path, case):
     w = SceneWriter(str(tmp_path))
     w.state(st)
     if isinstance(sc, tuple):
-        base, paints = sc
+        base, calls, paints = sc
         w.scene(base)
         w.lines.append("render")
-        w.paints(paints)
+        w.paints(calls)
         ref = O.render_paints(st, paints, base_scene=base)
     else:
         w.scene(sc)

@@ -153,6 +153,23 @@ def test_paints_match_reference(ref_lib):
         assert (got["ids"] != 0xFFFFFFFF).sum() > 1000
 
 
+def test_paint_after_view_change_matches_reference(ref_lib):
+    """paintMesh after setView uses the new view while the light stays where
+    render() placed it: the reference's own Renderer equals the frame as one
+    paint list whose later paints carry their modelview (MR_RS_MODELVIEW),
+    the form the mirrors hand to the library."""
+    import edge_scenes as E
+    st, calls, paints = E.view_change_paints()
+    got = O.render_paints(st, paints)
+    for clear in (False, True):
+        ref = O.ref_paint(st, calls, clear=clear)
+        assert _bits_equal(got["depth"], ref["depth"]), clear
+        assert _bits_equal(got["image"], ref["image"]), clear
+    # the view change moved what it drew: the same calls without it differ
+    flat = O.render_paints(st, [c for c in calls if not isinstance(c, tuple)])
+    assert not _bits_equal(flat["depth"], got["depth"])
+
+
 def test_paints_match_golden():
     """The oracle's paint sequence against the committed digests of the
     reference's own paintMesh / paintTriangle (tests/golden/paints.json)."""

@@ -145,12 +145,15 @@ def test_empty_frames(renderer):
 
 def _replay_paints(r, paints):
     """The paint records as Renderer calls: paintMesh (a mesh sharing the
-    arrays but carrying the paint's material where they differ), and
-    setMaterial + paintTriangle per triangle of a triangle run."""
+    arrays but carrying the paint's material where they differ),
+    setMaterial + paintTriangle per triangle of a triangle run, and setView
+    for a ("view", m) item."""
     from minirender_gb300 import abi
     from minirender_gb300.scene import TriMesh, Vertex
     for p in paints:
-        if p.flags & abi.MR_RS_MODELVIEW:
+        if isinstance(p, tuple):
+            r.setView(p[1])
+        elif p.flags & abi.MR_RS_MODELVIEW:
             r.setMaterial(p.material)
             m = p.mesh
             for t in range(m.indices.size // 3):
@@ -181,6 +184,26 @@ def test_paint_mesh_and_triangles(renderer, clear):
     gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
            "rgb8": renderer.getImageRGB8()}
     stats = compare(gpu, O.render_paints(st, paints), f"paints_clear{int(clear)}")
+    report(stats)
+    assert_parity(stats)
+    assert stats["covered"] > 5000
+
+
+def test_paint_after_view_change(renderer):
+    """render() of a scene, paintMesh, setView, then more paintMesh and a
+    paintTriangle run: the later meshes take the new view, the light stays
+    where render() placed it (pinned to the reference's Renderer on the
+    CPU)."""
+    import copy
+    st, calls, paints = E.view_change_paints(160, 120)
+    _, sc = W.config1(160, 120)
+    renderer.state = copy.deepcopy(st)  # setView below must not change the oracle's state
+    renderer.setScene(sc)
+    renderer.render()
+    _replay_paints(renderer, calls)
+    gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
+           "rgb8": renderer.getImageRGB8()}
+    stats = compare(gpu, O.render_paints(st, paints, base_scene=sc), "paints_view_change")
     report(stats)
     assert_parity(stats)
     assert stats["covered"] > 5000
