@@ -42,6 +42,8 @@ class Renderer:
         self._base = None                      # (renderables, count) of the last render()
         self._paints: list = []                # paintMesh / paintTriangle since then
         self._frame_view = None                # the view that places the frame's light
+        self._used = (set(), set())            # mesh keys / texture ids the frame being built uses
+        self._base_used = (set(), set())       # ... and those of the last render()
         self._dirty = False
         self.outputs = abi.MR_OUT_DEFAULT | abi.MR_OUT_RGB_F32
 
@@ -138,6 +140,7 @@ class Renderer:
     # ---- frame
     def _mesh_handle(self, mesh: sc.TriMesh) -> int:
         key = sc.geometry_key(mesh)
+        self._used[0].add(key)
         rec = self._meshes.get(key)
         if rec is not None and rec[2] is mesh.vertices:
             h, ver, _ = rec
@@ -150,6 +153,7 @@ class Renderer:
         return h
 
     def _texture_handle(self, tex: np.ndarray) -> int:
+        self._used[1].add(id(tex))
         rec = self._textures.get(id(tex))
         if rec is not None and rec[1] is tex:
             return rec[0]
@@ -174,10 +178,22 @@ class Renderer:
         self.state.ambient = getattr(self.scene, "ambientLight", np.float32(0.1))
         return self.state.to_c(), rs, n
 
+    def _prune(self):
+        """Frees the resident meshes and textures the frame just drawn does
+        not use (the caches hold the meshes of the last frame only)."""
+        meshes, textures = self._used
+        for key in [k for k in self._meshes if k not in meshes]:
+            self.ctx.free_mesh(self._meshes.pop(key)[0])
+        for key in [k for k in self._textures if k not in textures]:
+            self.ctx.free_texture(self._textures.pop(key)[0])
+
     def render(self):
         """Renderer::render (src/Renderer.cpp:311-332)."""
+        self._used = (set(), set())
         frame, rs, n = self.prepare()
         self.ctx.render(frame, rs, n, self.outputs)
+        self._base_used = (set(self._used[0]), set(self._used[1]))
+        self._prune()
         self._out = None
         self._rendered = True
         self._base = (rs, n)
@@ -188,6 +204,7 @@ class Renderer:
     def _flush_paints(self):
         """Renders the last render()'s renderables and the paints since."""
         base_rs, base_n = self._base if self._base is not None else (None, 0)
+        self._used = (set(self._base_used[0]), set(self._base_used[1])) if self._base is not None else (set(), set())
         prs = sc.paints_to_c(self._paints, self._mesh_handle, self._texture_handle)
         n = base_n + len(self._paints)
         rs = (abi.mr_renderable * max(1, n))()
@@ -199,6 +216,7 @@ class Renderer:
         if self._frame_view is not None:
             frame.view[:] = [float(x) for x in self._frame_view.reshape(16)]
         self.ctx.render(frame, rs, n, self.outputs)
+        self._prune()
         self._rendered = True
         self._dirty = False
         self._out = None

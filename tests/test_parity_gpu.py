@@ -209,6 +209,25 @@ def test_paint_after_view_change(renderer):
     assert stats["covered"] > 5000
 
 
+def test_resident_meshes_follow_the_frame(renderer):
+    """The mirror's caches hold the meshes and textures of the frame last
+    drawn: switching scenes frees the old scene's meshes, and drawing it
+    again re-sends them (the frames equal the oracle's each time)."""
+    st_a, sc_a = E.random_scene(3)
+    st_b, sc_b = W.config2(level=3, width=96, height=64, tex_size=16)
+    from minirender_gb300 import scene as S
+    for st, sc in ((st_a, sc_a), (st_b, sc_b), (st_a, sc_a)):
+        renderer.state = st
+        renderer.setScene(sc)
+        renderer.render()
+        flat = S.flatten(sc)
+        assert set(renderer._meshes) == {S.geometry_key(m) for m in flat.meshes}
+        assert len(renderer._textures) == len(flat.textures)
+        gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
+               "rgb8": renderer.getImageRGB8()}
+        assert_parity(compare(gpu, O.render(st, sc), "resident_follow"))
+
+
 def test_paint_over_rendered_scene(renderer):
     """render() of a scene, then paintTriangle runs over it: the scene's
     renderables come first in draw order."""
