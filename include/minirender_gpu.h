@@ -88,9 +88,22 @@ typedef struct mr_mesh_desc {
  *                    not applied (Renderer::paintTriangle's view-space
  *                    vertices are a one-triangle mesh with the identity here)
  *   MR_RS_NO_CLIP    no near-plane clipping (paintTriangle(..., world=false),
- *                    src/Renderer.cpp:163-173) */
-#define MR_RS_MODELVIEW 1
-#define MR_RS_NO_CLIP   2
+ *                    src/Renderer.cpp:163-173)
+ *   MR_RS_OWN_STATE  the renderable carries the switches its paint call saw
+ *                    (paintTriangle reads _lighting, _texturing and
+ *                    _lightIsPoint at the call, src/Renderer.cpp:264-289):
+ *                    MR_RS_LIGHTING, MR_RS_TEXTURING and MR_RS_POINT_LIGHT
+ *                    replace the frame's lighting, texturing and
+ *                    light_is_point for its fragments.  The light's position
+ *                    stays the frame's (placed as render() places it,
+ *                    :317-320, from the frame's view, light and
+ *                    light_is_point). */
+#define MR_RS_MODELVIEW   1
+#define MR_RS_NO_CLIP     2
+#define MR_RS_OWN_STATE   4
+#define MR_RS_LIGHTING    8
+#define MR_RS_TEXTURING   16
+#define MR_RS_POINT_LIGHT 32
 typedef struct mr_renderable {
     int32_t mesh;
     int32_t flags;

@@ -23,6 +23,10 @@ MR_NOALLOC_MAX_TRIANGLES = 1 << 22
 MR_NO_TRIANGLE = 0xFFFFFFFF
 MR_RS_MODELVIEW = 1  # mr_renderable.flags: transform is the modelview
 MR_RS_NO_CLIP = 2    # mr_renderable.flags: no near-plane clipping
+MR_RS_OWN_STATE = 4  # mr_renderable.flags: the three switches below replace the frame's
+MR_RS_LIGHTING = 8
+MR_RS_TEXTURING = 16
+MR_RS_POINT_LIGHT = 32
 
 MR_OUT_RGB8 = 1
 MR_OUT_DEPTH = 2

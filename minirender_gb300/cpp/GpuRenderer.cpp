@@ -93,7 +93,8 @@ void GpuRenderer::clear() {
     if (r.handle >= 0) mr_mesh_free(_ctx, r.handle);
   _runs.clear();
   _drawn = asl::Shared<Scene>();
-  _haveFrameView = false;
+  _haveFrame = false;
+  _clearBg = _bgcolor;  // the image clear() fills (src/Renderer.cpp:113-119)
   _rendered = false;
   _have = false;
 }
@@ -107,8 +108,7 @@ void GpuRenderer::render() {
   _scene->collectShapes(list, asl::Matrix4::identity());
   clear();
   _drawn = _scene;
-  _frameView = _view;  // the light is placed with it (src/Renderer.cpp:317-320)
-  _haveFrameView = true;
+  fixFrame();  // the light is placed now (src/Renderer.cpp:317-320)
   for (int i = 0; i < list.length(); i++) {
     Item it;
     it.mesh = list[i].mesh;
@@ -124,13 +124,11 @@ void GpuRenderer::render() {
 // the current view and `transform`, in the mesh's material or the default.
 void GpuRenderer::paintMesh(TriMesh* mesh, const asl::Matrix4& transform) {
   if (!mesh) throw GpuError(MR_E_INVALID, "paintMesh: null mesh");
-  if (!_haveFrameView) {
-    _frameView = _view;
-    _haveFrameView = true;
-  }
+  if (!_haveFrame) fixFrame();
   Item it;
   it.mesh = mesh;
   it.transform = transform;
+  it.flags = paintFlags();
   if (!sameMatrix(_view, _frameView)) {
     // the view changed since the frame's light was placed: the modelview
     // of this call, _view * transform (src/Renderer.cpp:337), composed as
@@ -141,7 +139,7 @@ void GpuRenderer::paintMesh(TriMesh* mesh, const asl::Matrix4& transform) {
     mr_mat4_mul(v, t, m);
     it.transform = asl::Matrix4(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], m[11], m[12],
                                 m[13], m[14], m[15]);
-    it.flags = MR_RS_MODELVIEW;
+    it.flags |= MR_RS_MODELVIEW;
   }
   it.material = mesh->material ? mesh->material : _defmaterial;
   _material = it.material;
@@ -155,11 +153,8 @@ void GpuRenderer::paintMesh(TriMesh* mesh, const asl::Matrix4& transform) {
 // near-plane clip.  Calls in a row that share material and clip mode form
 // one mesh whose modelview is the identity (MR_RS_MODELVIEW).
 void GpuRenderer::paintTriangle(const Vertex& a, const Vertex& b, const Vertex& c, bool world) {
-  const int32_t flags = MR_RS_MODELVIEW | (world ? 0 : MR_RS_NO_CLIP);
-  if (!_haveFrameView) {
-    _frameView = _view;
-    _haveFrameView = true;
-  }
+  if (!_haveFrame) fixFrame();
+  const int32_t flags = MR_RS_MODELVIEW | (world ? 0 : MR_RS_NO_CLIP) | paintFlags();
   asl::Shared<Material> mat = _material ? _material : _defmaterial;
   if (_items.empty() || _items.back().run < 0 || _items.back().flags != flags ||
       _items.back().material.operator->() != mat.operator->()) {
@@ -181,6 +176,25 @@ void GpuRenderer::paintTriangle(const Vertex& a, const Vertex& b, const Vertex& 
   }
   _rendered = false;
   _have = false;
+}
+
+// Renderer::render places the light with the view, light and light type of
+// the moment (src/Renderer.cpp:317-320); paints keep it until the next.
+void GpuRenderer::fixFrame() {
+  _frameView = _view;
+  _frameLight = _light;
+  _frameLightIsPoint = _lightIsPoint;
+  _frameLighting = _lighting;
+  _frameTexturing = _texturing;
+  _haveFrame = true;
+}
+
+// MR_RS_OWN_STATE and the switches of this paint call when they differ from
+// the frame's (paintTriangle reads them per call, src/Renderer.cpp:264-289).
+int32_t GpuRenderer::paintFlags() const {
+  if (_lighting == _frameLighting && _texturing == _frameTexturing && _lightIsPoint == _frameLightIsPoint) return 0;
+  return MR_RS_OWN_STATE | (_lighting ? MR_RS_LIGHTING : 0) | (_texturing ? MR_RS_TEXTURING : 0) |
+         (_lightIsPoint ? MR_RS_POINT_LIGHT : 0);
 }
 
 void GpuRenderer::meshChanged(TriMesh* mesh) {
@@ -281,17 +295,19 @@ mr_frame GpuRenderer::frame() const {
   f.width = _w;
   f.height = _h;
   rowMajor(_projection, f.projection);
-  rowMajor(_haveFrameView ? _frameView : _view, f.view);
-  f.light[0] = _light.x;
-  f.light[1] = _light.y;
-  f.light[2] = _light.z;
-  f.light_is_point = _lightIsPoint;
+  const bool fixed = _haveFrame;
+  rowMajor(fixed ? _frameView : _view, f.view);
+  const asl::Vec3& light = fixed ? _frameLight : _light;
+  f.light[0] = light.x;
+  f.light[1] = light.y;
+  f.light[2] = light.z;
+  f.light_is_point = fixed ? _frameLightIsPoint : _lightIsPoint;
   f.ambient = _drawn ? _drawn->ambientLight : (_scene ? _scene->ambientLight : 0.1f);
-  f.background[0] = _bgcolor.x;
-  f.background[1] = _bgcolor.y;
-  f.background[2] = _bgcolor.z;
-  f.lighting = _lighting;
-  f.texturing = _texturing;
+  f.background[0] = _clearBg.x;
+  f.background[1] = _clearBg.y;
+  f.background[2] = _clearBg.z;
+  f.lighting = fixed ? _frameLighting : _lighting;
+  f.texturing = fixed ? _frameTexturing : _texturing;
   f.save_normals = _saveNormals;
   return f;
 }

@@ -25,12 +25,13 @@
 //    is announced with textureChanged().
 //  * paintMesh / paintTriangle after render() or clear() are recorded and
 //    rendered with the frame, in call order, when an image is next read: the
-//    same pixels as painting them one after the other.  As in the
-//    reference, paintMesh uses the view current at the call, and the light
-//    is placed with the view of the last render() (or, with none since
-//    clear(), of the first paint).  The other state (size, projection,
-//    light, lighting, texturing, normals, background) is the frame's: the
-//    state when the image is read.
+//    same pixels as painting them one after the other.  State follows the
+//    reference call by call: paintMesh uses the view current at the call,
+//    every paint the lighting, texturing and light-type switches current at
+//    the call; the light is placed as the last render() placed it (with no
+//    render() since clear(), as the first paint finds it); the background
+//    is the one of the last clear() / render().  Projection and the normals
+//    switch are the frame's: the state when the image is read.
 //  * The caches hold the meshes and textures of the frame last drawn:
 //    entries the next frame does not use are freed.  A TriMesh or Material
 //    destroyed and replaced by another at the same address with arrays of
@@ -128,6 +129,8 @@ class GpuRenderer {
 
   void check(int status, const char* what) const;
   void prune();
+  void fixFrame();
+  int32_t paintFlags() const;
   int32_t meshHandle(TriMesh* m);
   int32_t textureHandle(const asl::Shared<Material>& mat);
   int32_t runHandle(TriangleRun& r);
@@ -138,8 +141,12 @@ class GpuRenderer {
   mr_ctx* _ctx = nullptr;
   int _w = 0, _h = 0;
   asl::Matrix4 _projection, _view;
-  asl::Matrix4 _frameView;      // the view that places the frame's light
-  bool _haveFrameView = false;
+  // the state that placed the frame's light (render(), or the first paint
+  // after clear()): view, light and the default switches of the frame
+  asl::Matrix4 _frameView;
+  asl::Vec3 _frameLight, _clearBg;
+  bool _frameLightIsPoint = false, _frameLighting = true, _frameTexturing = true;
+  bool _haveFrame = false;
   asl::Vec3 _light, _bgcolor;
   bool _lightIsPoint = false, _lighting = true, _texturing = true, _saveNormals = false;
   asl::Shared<Scene> _scene;

@@ -276,6 +276,19 @@ MR_API int mr_set_profiling(mr_ctx* c, int on) {
   return MR_OK;
 }
 
+static constexpr int32_t kRenderableFlags =
+    MR_RS_MODELVIEW | MR_RS_NO_CLIP | MR_RS_OWN_STATE | MR_RS_LIGHTING | MR_RS_TEXTURING | MR_RS_POINT_LIGHT;
+
+// The switches paintTriangle reads for a renderable's fragments
+// (src/Renderer.cpp:264-289): its own (MR_RS_OWN_STATE) or the frame's.
+// Sets R.lit and R.point; returns whether texturing is on.
+static bool switches(int32_t flags, const mr_frame& f, DevRenderable& R) {
+  const bool own = (flags & MR_RS_OWN_STATE) != 0;
+  R.lit = own ? (flags & MR_RS_LIGHTING) != 0 : f.lighting != 0;
+  R.point = own ? (flags & MR_RS_POINT_LIGHT) != 0 : f.light_is_point != 0;
+  return own ? (flags & MR_RS_TEXTURING) != 0 : f.texturing != 0;
+}
+
 // Copies the mesh arrays on st and checks the indices there, or -- when st
 // is the upload stream (or the caller defers the check), which carries
 // copies only so the next transfer never waits for SMs -- later, before the
@@ -570,7 +583,7 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     int32_t t = rs[i].material.texture;
     if (t >= 0 && (t >= (int32_t)c->textures.size() || !c->textures[t].live))
       return fail(c, MR_E_HANDLE, "material refers to an unknown texture");
-    if (rs[i].flags & ~(MR_RS_MODELVIEW | MR_RS_NO_CLIP)) return fail(c, MR_E_INVALID, "unknown renderable flags");
+    if (rs[i].flags & ~kRenderableFlags) return fail(c, MR_E_INVALID, "unknown renderable flags");
     total += (uint64_t)c->meshes[h].d.n_tri;
   }
   if (total >= ((uint64_t)1 << 31)) return fail(c, MR_E_INVALID, "more than 2^31-1 triangles in one frame");
@@ -612,6 +625,7 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     memcpy(R.nm, nm, sizeof(R.nm));
     R.mesh = m.d;
     R.no_clip = (rs[i].flags & MR_RS_NO_CLIP) ? 1 : 0;
+    const bool texturing = switches(rs[i].flags, *f, R);
     R.tri_base = base;
     c->h_tri_base[i] = base;
     base += (uint32_t)m.d.n_tri;
@@ -632,7 +646,7 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
     R.tex8 = nullptr;
     R.texf = nullptr;
     R.tex_rows = R.tex_cols = 0;
-    if (f->texturing && M.texture >= 0) {
+    if (texturing && M.texture >= 0) {
       const TexRec& T = c->textures[M.texture];
       R.has_tex = 1;
       R.tex_rows = T.rows;
@@ -1056,7 +1070,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
     int32_t t = rs[i].material.texture;
     if (t >= 0 && (t >= (int32_t)c->textures.size() || !c->textures[t].live))
       return fail(c, MR_E_HANDLE, "material refers to an unknown texture");
-    if (rs[i].flags & ~(MR_RS_MODELVIEW | MR_RS_NO_CLIP)) return fail(c, MR_E_INVALID, "unknown renderable flags");
+    if (rs[i].flags & ~kRenderableFlags) return fail(c, MR_E_INVALID, "unknown renderable flags");
     tris += (uint64_t)c->meshes[h].d.n_tri;
     verts += (uint64_t)c->meshes[h].d.n_pos;
     nrms += (uint64_t)c->meshes[h].d.n_nrm;
@@ -1151,6 +1165,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
       memcpy(R.nm, nm, sizeof(R.nm));
       R.mesh = m.d;
       R.no_clip = (rs[i].flags & MR_RS_NO_CLIP) ? 1 : 0;
+      const bool texturing = switches(rs[i].flags, *f, R);
       R.tri_base = tb[i];
       R.vert_base = vbase[i];
       R.nrm_base = nbase[i];
@@ -1160,7 +1175,7 @@ int batch_stage(mr_ctx* c, BatchSlot& B, const mr_batch_scene* sc, int32_t n_sce
       memcpy(R.specular, M.specular, sizeof(R.specular));
       memcpy(R.emissive, M.emissive, sizeof(R.emissive));
       R.shininess = M.shininess;
-      if (f->texturing && M.texture >= 0) {
+      if (texturing && M.texture >= 0) {
         const TexRec& T = c->textures[M.texture];
         R.has_tex = 1;
         R.tex_rows = T.rows;

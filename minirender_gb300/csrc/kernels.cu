@@ -476,10 +476,10 @@ __device__ __forceinline__ void shade(const View& V, const DevRenderable& R, con
       color = v3(R.texf[o], R.texf[o + 1], R.texf[o + 2]);
   }
   value = v3(R.emissive[0], R.emissive[1], R.emissive[2]);
-  if (V.lighting) {
+  if (R.lit) {
     V3 position = add3(add3(ks3(k0, vc[0].pos), ks3(k1, vc[1].pos)), ks3(k2, vc[2].pos));
     V3 LD = v3(V.lightdir[0], V.lightdir[1], V.lightdir[2]);
-    V3 lightdir = V.point ? normalized3(sub3(LD, position)) : LD;
+    V3 lightdir = R.point ? normalized3(sub3(LD, position)) : LD;
     V3 normal = add3(add3(ks3(k0, vc[0].nrm), ks3(k1, vc[1].nrm)), ks3(k2, vc[2].nrm));
     float sdiff = maxr(0.0f, dot3(normal, lightdir)) / len3(normal) + V.ambient;
     value = add3(value, ks3(sdiff, color));

@@ -51,6 +51,8 @@ struct DevRenderable {
   uint32_t scene;       // frame (scene) this renderable belongs to (batches)
   int32_t has_tex;      // texturing on and the material has a texture
   int32_t no_clip;      // MR_RS_NO_CLIP: no near-plane clipping
+  int32_t lit;          // lighting on for its fragments (the frame's or its paint call's)
+  int32_t point;        // point light for its fragments (the frame's or its paint call's)
   float diffuse[3], specular[3], emissive[3], shininess;
   const uint8_t* tex8;  // rows x cols x 3 bytes (decoded b/255), or
   const float* texf;    // rows x cols x 3 floats

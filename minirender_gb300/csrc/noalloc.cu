@@ -106,6 +106,8 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   M.n_tri = d->n_indices / 3;
   M.has_uv = has_uv;
   R.tri_base = 0;
+  R.lit = f->lighting != 0;
+  R.point = f->light_is_point != 0;
   memcpy(R.diffuse, mat->diffuse, sizeof(R.diffuse));
   memcpy(R.specular, mat->specular, sizeof(R.specular));
   memcpy(R.emissive, mat->emissive, sizeof(R.emissive));

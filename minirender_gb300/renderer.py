@@ -11,14 +11,18 @@ results back.
 reference's do: after ``clear()`` (or ``render()``) the paints are recorded
 and the next getter renders the scene's renderables and the paints, in call
 order, as one frame -- the same pixels as painting them one after the other
-(later fragments win only with a strictly smaller depth).  As in the
-reference, ``paintMesh`` uses the view current at the call and the light is
-placed with the view of the last ``render()`` (or, with none since
-``clear()``, of the first paint).  The other state (size, projection, light,
-lighting, texturing, background, normals) is the frame's: the state when the
-frame is read.
+(later fragments win only with a strictly smaller depth).  State follows the
+reference call by call: ``paintMesh`` uses the view current at the call, and
+every paint the lighting, texturing and light-type switches current at the
+call; the light is placed as the last ``render()`` placed it (with its view,
+light and light type; with no ``render()`` since ``clear()``, as the first
+paint finds them); the background is the one of the last ``clear()`` /
+``render()``.  Projection and the normals switch are the frame's: the state
+when the frame is read.
 """
 from __future__ import annotations
+
+import copy
 
 from typing import Dict, Optional
 
@@ -41,7 +45,8 @@ class Renderer:
         self._rendered = False
         self._base = None                      # (renderables, count) of the last render()
         self._paints: list = []                # paintMesh / paintTriangle since then
-        self._frame_view = None                # the view that places the frame's light
+        self._frame_state: Optional[FrameState] = None  # state that placed the frame's light
+        self._clear_bg = None                  # background of the last clear() / render()
         self._used = (set(), set())            # mesh keys / texture ids the frame being built uses
         self._base_used = (set(), set())       # ... and those of the last render()
         self._dirty = False
@@ -92,16 +97,27 @@ class Renderer:
         self._rendered = False
         self._base = None
         self._paints = []
-        self._frame_view = None
+        self._frame_state = None
+        self._clear_bg = np.asarray(self.state.background, np.float32).copy()
         self._dirty = False
 
-    def _paint_view(self) -> np.ndarray:
-        """The view at a paint call; the first paint after clear() fixes the
-        frame's view."""
-        view = np.asarray(self.state.view, np.float32).reshape(4, 4)
-        if self._frame_view is None:
-            self._frame_view = view.copy()
-        return view
+    def _frame(self) -> FrameState:
+        """The state the frame's light was placed with: the last render()'s,
+        or, with none since clear(), the first paint's."""
+        if self._frame_state is None:
+            self._frame_state = copy.deepcopy(self.state)
+        return self._frame_state
+
+    def _paint_flags(self) -> int:
+        """MR_RS_OWN_STATE and the switches of this paint call when they
+        differ from the frame's (src/Renderer.cpp:264-289 reads them per
+        call)."""
+        f, s = self._frame(), self.state
+        cur = (bool(s.lighting), bool(s.texturing), bool(s.light_is_point))
+        if cur == (bool(f.lighting), bool(f.texturing), bool(f.light_is_point)):
+            return 0
+        return (abi.MR_RS_OWN_STATE | (abi.MR_RS_LIGHTING if cur[0] else 0) |
+                (abi.MR_RS_TEXTURING if cur[1] else 0) | (abi.MR_RS_POINT_LIGHT if cur[2] else 0))
 
     def paintMesh(self, mesh: sc.TriMesh, transform=None):
         """Renderer::paintMesh (src/Renderer.cpp:334-381): the mesh with the
@@ -110,15 +126,16 @@ class Renderer:
         mat = mesh.material if mesh.material is not None else sc.Material()
         self._material = mat
         xf = sc.identity() if transform is None else transform
-        view = self._paint_view()
-        if view.tobytes() == self._frame_view.tobytes():
-            self._paints.append(sc.Paint(mesh, xf, mat, 0))
+        view = np.asarray(self.state.view, np.float32).reshape(4, 4)
+        flags = self._paint_flags()
+        if view.tobytes() == np.asarray(self._frame().view, np.float32).reshape(4, 4).tobytes():
+            self._paints.append(sc.Paint(mesh, xf, mat, flags))
         else:
             # the view changed since the frame's light was placed: this
             # call's modelview, _view * transform (src/Renderer.cpp:337),
             # composed as the library composes it
             mv = capi.mat4_mul(view, np.asarray(xf, np.float32).reshape(4, 4))
-            self._paints.append(sc.Paint(mesh, mv, mat, abi.MR_RS_MODELVIEW))
+            self._paints.append(sc.Paint(mesh, mv, mat, abi.MR_RS_MODELVIEW | flags))
         self._dirty = True
 
     def paintTriangle(self, a: sc.Vertex, b: sc.Vertex, c: sc.Vertex, world: bool = True):
@@ -126,13 +143,13 @@ class Renderer:
         of view-space vertices in the current material; world=False skips the
         near-plane clipping."""
         mat = self._material if self._material is not None else sc.Material()
-        self._paint_view()
-        flags = abi.MR_RS_MODELVIEW | (0 if world else abi.MR_RS_NO_CLIP)
+        flags = abi.MR_RS_MODELVIEW | (0 if world else abi.MR_RS_NO_CLIP) | self._paint_flags()
         last = self._paints[-1] if self._paints else None
         if last is not None and last.flags == flags and last.material is mat and getattr(last, "run", False):
             sc.append_triangle(last, a, b, c)
         else:
             p = sc.triangle_paint(a, b, c, mat, world)
+            p.flags = flags  # with the switches of this call
             p.run = True
             self._paints.append(p)
         self._dirty = True
@@ -198,7 +215,8 @@ class Renderer:
         self._rendered = True
         self._base = (rs, n)
         self._paints = []
-        self._frame_view = np.asarray(self.state.view, np.float32).reshape(4, 4).copy()
+        self._frame_state = copy.deepcopy(self.state)
+        self._clear_bg = np.asarray(self.state.background, np.float32).copy()
         self._dirty = False
 
     def _flush_paints(self):
@@ -212,14 +230,26 @@ class Renderer:
             rs[i] = base_rs[i]
         for j in range(len(self._paints)):
             rs[base_n + j] = prs[j]
-        frame = self.state.to_c()
-        if self._frame_view is not None:
-            frame.view[:] = [float(x) for x in self._frame_view.reshape(16)]
+        frame = self._frame_c()
         self.ctx.render(frame, rs, n, self.outputs)
         self._prune()
         self._rendered = True
         self._dirty = False
         self._out = None
+
+    def _frame_c(self):
+        """mr_frame of a flush: the light, its view and the default switches
+        of the frame, the background of the last clear(), the rest current."""
+        frame = self.state.to_c()
+        f = self._frame()
+        frame.view[:] = [float(x) for x in np.asarray(f.view, np.float32).reshape(16)]
+        frame.light[:] = [float(x) for x in np.asarray(f.light, np.float32).reshape(3)]
+        frame.light_is_point = int(bool(f.light_is_point))
+        frame.lighting = int(bool(f.lighting))
+        frame.texturing = int(bool(f.texturing))
+        if self._clear_bg is not None:
+            frame.background[:] = [float(x) for x in self._clear_bg]
+        return frame
 
     def _read(self) -> dict:
         if self._dirty:
@@ -234,7 +264,7 @@ class Renderer:
     def _cleared(self) -> dict:
         H, W = self.state.height, self.state.width
         img = np.empty((H, W, 3), np.float32)
-        img[:] = np.asarray(self.state.background, np.float32)
+        img[:] = np.asarray(self.state.background if self._clear_bg is None else self._clear_bg, np.float32)
         out = {"image": img, "depth": np.full((H, W), 1e11, np.float32),
                "ids": np.full((H, W), abi.MR_NO_TRIANGLE, np.uint32)}
         out["rgb8"] = np.clip(img * np.float32(255), 0, 255).astype(np.uint8)

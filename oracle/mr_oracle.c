@@ -421,6 +421,17 @@ int mro_render(const mr_frame* f, const mr_renderable* rs, int32_t n, const mr_m
     for (int32_t r = 0; r < n; r++) {
         if (rs[r].mesh < 0 || rs[r].mesh >= n_meshes) return MR_E_HANDLE;
         const mr_mesh_desc* m = &meshes[rs[r].mesh];
+        /* the switches of the renderable's paint call (MR_RS_OWN_STATE) or
+           the frame's; the light's position stays the frame's (:264-289) */
+        if (rs[r].flags & MR_RS_OWN_STATE) {
+            F.lighting = (rs[r].flags & MR_RS_LIGHTING) != 0;
+            F.texturing = (rs[r].flags & MR_RS_TEXTURING) != 0;
+            F.point = (rs[r].flags & MR_RS_POINT_LIGHT) != 0;
+        } else {
+            F.lighting = f->lighting;
+            F.texturing = f->texturing;
+            F.point = f->light_is_point;
+        }
         F.mat = &rs[r].material;
         F.tex = NULL;
         if (rs[r].material.texture >= 0) {

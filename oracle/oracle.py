@@ -342,7 +342,10 @@ def ref_paint(state: FrameState, paints, clear: bool = False) -> dict:
     """The reference Renderer itself: render() of an empty scene (the state
     paintMesh uses), clear() if asked, then the paints in order -- paintMesh
     for a scene.Paint without MR_RS_MODELVIEW, setMaterial + paintTriangle
-    per triangle of a paintTriangle run, setView(m) for an item ("view", m)."""
+    per triangle of a paintTriangle run, and for the state items between
+    them: setView(m) for ("view", m), setLighting(b) for ("lighting", b),
+    setTexturing(b) for ("texturing", b), setLight(v, point) for
+    ("light", v, point), setBackground(rgb) for ("background", rgb)."""
     L = ref_lib()
     if L is None:
         raise RuntimeError("reference build unavailable")
@@ -356,9 +359,22 @@ def ref_paint(state: FrameState, paints, clear: bool = False) -> dict:
         return tex_ix[id(t)]
 
     for p in paints:
-        if isinstance(p, tuple) and p[0] == "view":
-            kind.append(2); mesh.append(-1); xf.append(np.asarray(p[1], np.float32).reshape(4, 4))
-            mats.append(abi.mr_material()); world.append(1); tri.append(np.zeros(24, np.float32))
+        if isinstance(p, tuple):
+            m16 = np.zeros(16, np.float32)
+            flag = 1
+            if p[0] == "view":
+                k, m16[:] = 2, np.asarray(p[1], np.float32).reshape(16)
+            elif p[0] in ("lighting", "texturing"):
+                k, flag = (3 if p[0] == "lighting" else 4), int(bool(p[1]))
+            elif p[0] == "light":
+                k, flag = 5, int(bool(p[2]))
+                m16[:3] = np.asarray(p[1], np.float32).reshape(3)
+            elif p[0] == "background":
+                k, m16[:3] = 6, np.asarray(p[1], np.float32).reshape(3)
+            else:
+                raise ValueError(f"unknown state item {p[0]!r}")
+            kind.append(k); mesh.append(-1); xf.append(m16.reshape(4, 4))
+            mats.append(abi.mr_material()); world.append(flag); tri.append(np.zeros(24, np.float32))
             continue
         m = abi.mr_material()
         tex = p.material.texture

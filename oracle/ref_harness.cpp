@@ -330,7 +330,10 @@ static Shared<Material> make_material(const mr_material& mm, const RefTexture* t
 // then n_ops paints in order: kind 0 = paintMesh(meshes[mesh[i]] with
 // material[i], transform[16 i..]), kind 1 = setMaterial(material[i]) and
 // paintTriangle of tri[24 i..] (3 x position, normal, uv) with world[i],
-// kind 2 = setView(transform[16 i..]) for the paints after it.
+// kind 2 = setView(transform[16 i..]), kind 3 = setLighting(world[i]),
+// kind 4 = setTexturing(world[i]), kind 5 = setLight(transform[16 i..16 i+2],
+// point = world[i]), kind 6 = setBackground(transform[16 i..16 i+2]); each
+// for the calls after it.
 int ref_paint(const mr_frame* f, const mr_mesh_desc* meshes, int32_t n_meshes, const RefTexture* tex,
               int32_t n_tex, int do_clear, int32_t n_ops, const int32_t* kind, const int32_t* mesh,
               const float* transform, const mr_material* material, const float* tri, const int32_t* world,
@@ -350,8 +353,25 @@ int ref_paint(const mr_frame* f, const mr_mesh_desc* meshes, int32_t n_meshes, c
   if (do_clear) r.clear();
   std::vector<Shared<TriMesh>> keep;
   for (int32_t i = 0; i < n_ops; i++) {
+    const float* q16 = transform + 16 * i;
     if (kind[i] == 2) {
-      r.setView(to_m4(transform + 16 * i));
+      r.setView(to_m4(q16));
+      continue;
+    }
+    if (kind[i] == 3) {
+      r.setLighting(world[i] != 0);
+      continue;
+    }
+    if (kind[i] == 4) {
+      r.setTexturing(world[i] != 0);
+      continue;
+    }
+    if (kind[i] == 5) {
+      r.setLight(Vec3(q16[0], q16[1], q16[2]), world[i] != 0);
+      continue;
+    }
+    if (kind[i] == 6) {
+      r.setBackground(Vec3(q16[0], q16[1], q16[2]));
       continue;
     }
     Shared<Material> mat = make_material(material[i], tex, n_tex);

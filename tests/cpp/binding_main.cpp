@@ -8,6 +8,7 @@
 // scene.txt holds one command per line, executed in order:
 //   size W H | projection p0..p15 | view v0..v15 | light x y z point
 //   background r g b | switches lighting texturing save_normals
+//   lighting B | texturing B       (setLighting / setTexturing alone)
 //   texture K ROWS COLS FILE       (float32 RGB texels, as loadPPM leaves them)
 //   mesh K FILE NV NN NT NI NNI NTI (float32 vertices, normals, texcoords,
 //                                    then int32 indices, normalsI, texcoordsI)
@@ -152,6 +153,11 @@ int run(const char* scene_file) {
       r.setTexturing(t != 0);
       r.setSaveNormals(n != 0);
       save_normals = n != 0;
+    } else if (cmd == "lighting" || cmd == "texturing") {
+      int on;
+      in >> on;
+      if (cmd == "lighting") r.setLighting(on != 0);
+      else r.setTexturing(on != 0);
     } else if (cmd == "texture") {
       int k, rows, cols;
       std::string path;

@@ -256,6 +256,34 @@ def view_change_paints(w=160, h=120):
     return st, calls, paints
 
 
+def state_change_paints(w=160, h=120):
+    """Paints between setLighting / setTexturing / setLight / setBackground
+    calls (src/Renderer.cpp:163-381: paintTriangle reads the lighting,
+    texturing and light-type switches at the call; the light's position is
+    the one render() computed; the background is filled by clear()).
+    Returns (state, calls, paints) as view_change_paints does: in `paints`
+    a paint whose switches differ from the frame's carries MR_RS_OWN_STATE
+    and its own switches."""
+    from minirender_gb300.scene import Paint
+    st, seq = paint_sequence(w, h)
+    sphere_paint, quad_paint, run, again = seq[0], seq[1], seq[2], seq[4]
+    t3 = pj.mat_mul(pj.translate(0.9, -0.5, 0.3), pj.scale(0.5))
+    last = Paint(sphere_paint.mesh, t3, Material(diffuse=(0.9, 0.2, 0.2), specular=(1, 1, 1), shininess=16))
+    own, lit, tex, point = abi.MR_RS_OWN_STATE, abi.MR_RS_LIGHTING, abi.MR_RS_TEXTURING, abi.MR_RS_POINT_LIGHT
+    calls = [sphere_paint,
+             ("lighting", False), quad_paint,                      # unlit, textured
+             ("texturing", False), ("lighting", True), run,        # lit, untextured
+             ("light", (-1.0, 2.0, 3.0), False), last,             # render()'s light used as a direction
+             ("background", (0.5, 0.5, 0.5)),                      # after clear(): no effect
+             ("texturing", True), ("light", (2.0, 3.0, 4.0), True), again]  # the frame's switches again
+    paints = [sphere_paint,
+              Paint(quad_paint.mesh, quad_paint.transform, quad_paint.material, own | tex | point),
+              Paint(run.mesh, run.transform, run.material, run.flags | own | lit | point),
+              Paint(last.mesh, last.transform, last.material, own | lit),
+              again]
+    return st, calls, paints
+
+
 def random_scene(seed: int):
     """Seeded random scene for fuzzing the whole path: 1-4 meshes of 10-250
     triangles, each either a soup (every corner its own vertex) or indexed

@@ -196,3 +196,21 @@ def test_noalloc_limits_checked_before_device_work(product_lib):
     d = abi.mr_mesh_desc()
     for w, h in ((abi.MR_NOALLOC_MAX_SIDE + 1, 16), (2048, 2048)):
         assert _noalloc_call(product_lib, d, w, h) == abi.MR_E_NOALLOC_LIMIT
+
+
+def test_header_constants_match_abi():
+    """Every integer #define of include/minirender_gpu.h that the Python ABI
+    mirrors has the same value there; the renderable flags are all mirrored."""
+    import re
+    from minirender_gb300 import abi
+    with open(os.path.join(ROOT, "include", "minirender_gpu.h")) as f:
+        txt = f.read()
+    # plain literals only (a value written as an expression is skipped)
+    defs = dict(re.findall(r"^#define\s+(MR_\w+)\s+\(?(-?(?:0x[0-9a-fA-F]+|\d+))\)?[ \t]*(?:/\*.*)?$", txt, re.M))
+    assert {k for k in defs if k.startswith("MR_RS_")} <= set(dir(abi))
+    checked = 0
+    for name, value in defs.items():
+        if hasattr(abi, name):
+            assert getattr(abi, name) == int(value, 0), name
+            checked += 1
+    assert checked >= 10

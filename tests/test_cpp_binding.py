@@ -119,8 +119,17 @@ class SceneWriter:
 
     def paints(self, paints):
         for p in paints:
-            if isinstance(p, tuple):  # ("view", m): setView
-                self.lines.append(f"view {_floats(list(np.asarray(p[1], np.float32).reshape(16)))}")
+            if isinstance(p, tuple):  # state calls between paints
+                if p[0] == "view":
+                    self.lines.append(f"view {_floats(list(np.asarray(p[1], np.float32).reshape(16)))}")
+                elif p[0] in ("lighting", "texturing"):
+                    self.lines.append(f"{p[0]} {int(bool(p[1]))}")
+                elif p[0] == "light":
+                    self.lines.append(f"light {_floats(p[1])} {int(bool(p[2]))}")
+                elif p[0] == "background":
+                    self.lines.append(f"background {_floats(p[1])}")
+                else:
+                    raise ValueError(p[0])
                 continue
             tex = self.texture(p.material.texture) if p.material.texture is not None else -1
             if p.flags & abi.MR_RS_MODELVIEW:
@@ -191,6 +200,8 @@ def _cases():
     yield "render_then_paints", st, (sc, paints, paints)
     st, calls, paints = E.view_change_paints(160, 120)
     yield "paints_after_view_change", st, (W.config1(160, 120)[1], calls, paints)
+    st, calls, paints = E.state_change_paints(160, 120)
+    yield "paints_after_state_changes", st, (W.config1(160, 120)[1], calls, paints)
 
 
 def _fix(case):

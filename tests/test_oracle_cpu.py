@@ -5,6 +5,8 @@ import glob
 import os
 
 import numpy as np
+
+from minirender_gb300 import abi
 import pytest
 
 import edge_scenes as E
@@ -168,6 +170,25 @@ def test_paint_after_view_change_matches_reference(ref_lib):
     # the view change moved what it drew: the same calls without it differ
     flat = O.render_paints(st, [c for c in calls if not isinstance(c, tuple)])
     assert not _bits_equal(flat["depth"], got["depth"])
+
+
+def test_paint_after_state_changes_matches_reference(ref_lib):
+    """setLighting / setTexturing / setLight / setBackground between paints:
+    the reference's own Renderer equals the frame as one paint list whose
+    paints carry the switches of their call (MR_RS_OWN_STATE), with the
+    light where render() placed it and the background of clear()."""
+    import edge_scenes as E
+    st, calls, paints = E.state_change_paints()
+    got = O.render_paints(st, paints)
+    for clear in (False, True):
+        ref = O.ref_paint(st, calls, clear=clear)
+        assert _bits_equal(got["depth"], ref["depth"]), clear
+        assert _bits_equal(got["image"], ref["image"]), clear
+    # the switches changed what was drawn: the same paints under the frame's differ
+    keep = abi.MR_RS_MODELVIEW | abi.MR_RS_NO_CLIP
+    plain = O.render_paints(st, [type(p)(p.mesh, p.transform, p.material, p.flags & keep) for p in paints])
+    assert not _bits_equal(plain["image"], got["image"])
+    assert _bits_equal(plain["depth"], got["depth"])
 
 
 def test_paints_match_golden():

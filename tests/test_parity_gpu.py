@@ -151,8 +151,19 @@ def _replay_paints(r, paints):
     from minirender_gb300 import abi
     from minirender_gb300.scene import TriMesh, Vertex
     for p in paints:
-        if isinstance(p, tuple):
-            r.setView(p[1])
+        if isinstance(p, tuple):  # state calls between paints
+            if p[0] == "view":
+                r.setView(p[1])
+            elif p[0] == "lighting":
+                r.setLighting(p[1])
+            elif p[0] == "texturing":
+                r.setTexturing(p[1])
+            elif p[0] == "light":
+                r.setLight(p[1], p[2])
+            elif p[0] == "background":
+                r.setBackground(p[1])
+            else:
+                raise ValueError(p[0])
         elif p.flags & abi.MR_RS_MODELVIEW:
             r.setMaterial(p.material)
             m = p.mesh
@@ -209,6 +220,26 @@ def test_paint_after_view_change(renderer):
     assert stats["covered"] > 5000
 
 
+def test_paint_after_state_changes(renderer):
+    """setLighting / setTexturing / setLight / setBackground between paints
+    after render(): each paint shades with the switches of its call, the
+    light stays where render() placed it, the background is render()'s
+    (pinned to the reference's Renderer on the CPU)."""
+    import copy
+    st, calls, paints = E.state_change_paints(160, 120)
+    _, sc = W.config1(160, 120)
+    renderer.state = copy.deepcopy(st)
+    renderer.setScene(sc)
+    renderer.render()
+    _replay_paints(renderer, calls)
+    gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
+           "rgb8": renderer.getImageRGB8()}
+    stats = compare(gpu, O.render_paints(st, paints, base_scene=sc), "paints_state_changes")
+    report(stats)
+    assert_parity(stats)
+    assert stats["covered"] > 5000
+
+
 def test_resident_meshes_follow_the_frame(renderer):
     """The mirror's caches hold the meshes and textures of the frame last
     drawn: switching scenes frees the old scene's meshes, and drawing it
@@ -252,7 +283,8 @@ def test_unknown_renderable_flags_rejected(renderer):
     renderer.state = st
     renderer.setScene(sc)
     frame, rs, n = renderer.prepare()
-    rs[0].flags = 4
+    from minirender_gb300 import abi
+    rs[0].flags = abi.MR_RS_POINT_LIGHT << 1  # the first bit no flag uses
     with pytest.raises(capi.MRError):
         renderer.ctx.render(frame, rs, n, renderer.outputs)
     rs[0].flags = 0
