@@ -210,11 +210,15 @@ def collect_shapes(flat: sc.Flat):
     return out, n.value
 
 
-def render(state: FrameState, scene: sc.SceneNode, normals: bool = False) -> dict:
+def render(state: FrameState, scene: sc.SceneNode, normals: bool = False, flags=None) -> dict:
     """The C restatement: image (H,W,3) f32, depth (H,W) f32, ids (H,W) u32,
-    rgb8 (H,W,3) u8 and optionally normals."""
+    rgb8 (H,W,3) u8 and optionally normals.  `flags` (one int per renderable
+    in collectShapes order) are or-ed into the renderables' flags."""
     flat = sc.flatten(scene)
     rs, n = collect_shapes(flat)
+    if flags is not None:
+        for i in range(n):
+            rs[i].flags |= int(flags[i])
     meshes = sc.mesh_descs(flat.meshes)
     tex, keep = _float_textures(flat.textures)
     f = state.to_c()

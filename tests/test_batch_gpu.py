@@ -143,6 +143,43 @@ def test_batch_of_random_scenes(batch):
     batch.ctx.set_batch_graphs(True)
 
 
+def _switch_flags(k: int) -> int:
+    """A cycle of renderable switch combinations (MR_RS_OWN_STATE with and
+    without lighting, texturing and point light; 0 = the frame's)."""
+    from minirender_gb300 import abi
+    own, lit, tex, pt = abi.MR_RS_OWN_STATE, abi.MR_RS_LIGHTING, abi.MR_RS_TEXTURING, abi.MR_RS_POINT_LIGHT
+    return (0, own | tex, own | lit, own | lit | tex | pt, own, own | lit | pt, own | tex | pt)[k % 7]
+
+
+def test_batch_with_paint_switches(batch):
+    """Renderables carrying their paint call's switches (MR_RS_OWN_STATE:
+    lighting, texturing, light type) in a batch equal the oracle's render
+    with the same flags, with and without graph replay."""
+    items = [W.config4_scene(s) for s in range(3)]
+    items.append(W.config2(level=5, width=320, height=200, tex_size=64))
+    items.append(E.ALL["near_clip"]())
+    items.append(E.ALL["texture_wrap"]())
+    scenes, ns, rs, nr = batch.prepare(items)
+    refs = []
+    for s, (st, sc) in enumerate(items):
+        first, n = scenes[s].first_renderable, scenes[s].n_renderables
+        for i in range(n):
+            rs[first + i].flags |= _switch_flags(first + i)
+        refs.append(O.render(st, sc, flags=[_switch_flags(first + i) for i in range(n)]))
+    for graphs in (False, True):
+        batch.ctx.set_batch_graphs(graphs)
+        batch.ctx.render_batch(scenes, ns, rs, nr, batch.outputs)
+        out = []
+        for i, ref in enumerate(refs):
+            got = batch.read(i)
+            got["image"] = ref["image"]
+            stats = compare(got, ref, f"batch_switches_g{int(graphs)}_{i}")
+            out.append(stats)
+            assert_parity(stats)
+        report(out, "batch")
+    batch.ctx.set_batch_graphs(True)
+
+
 def test_batch_with_empty_scenes(batch):
     """Scenes without renderables or with empty meshes come out as background
     (and do not disturb the other scenes of the batch)."""
