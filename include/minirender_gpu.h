@@ -408,6 +408,10 @@ MR_API int mr_ppm_save(const char* path, const uint8_t* rgb8, int32_t rows, int3
 /* saveSTL (src/io.cpp:155-183): binary STL of the mesh's triangles under a
  * row-major transform (NULL: identity). */
 MR_API int mr_stl_save(const char* path, const mr_mesh_desc* mesh, const float* transform);
+/* saveXYZ (src/io.cpp:417-431): the points of a rows x cols x 3 float image
+ * (mr_read_range_image's) whose z < -1e-5, one "x y z" line each (printf
+ * "%f"), in row order, after transform (row-major; NULL = identity). */
+MR_API int mr_xyz_save(const char* path, const float* xyz, int32_t rows, int32_t cols, const float* transform);
 
 /* ---- host helpers (no device work) -------------------------------------- */
 /* Scene::collectShapes (src/Scene.cpp:13-36) over a pre-order node array.

@@ -59,6 +59,7 @@ _SIGS = {
     "mr_ppm_load": ([C.c_char_p, _P, C.c_int64, _P, _P], C.c_int),
     "mr_ppm_save": ([C.c_char_p, _P, C.c_int32, C.c_int32], C.c_int),
     "mr_stl_save": ([C.c_char_p, _P, _P], C.c_int),
+    "mr_xyz_save": ([C.c_char_p, _P, C.c_int32, C.c_int32, _P], C.c_int),
     "mr_set_batch_graphs": ([_P, C.c_int], C.c_int),
     "mr_render_batch": ([_P, _P, _I, _P, _I, _I], C.c_int),
     "mr_read_batch": ([_P, _I, _P, _P, _P], C.c_int),

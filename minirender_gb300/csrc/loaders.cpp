@@ -997,4 +997,26 @@ MR_API int mr_stl_save(const char* path, const mr_mesh_desc* d, const float* tra
   return w == buf.size() ? MR_OK : MR_E_IO;
 }
 
+// saveXYZ (src/io.cpp:417-431): one "x y z" line (printf %f) per point of the
+// rows x cols image whose z < -1e-5, in row order, after transform
+// (row-major, NULL = identity; m * p, no w divide).
+MR_API int mr_xyz_save(const char* path, const float* xyz, int32_t rows, int32_t cols, const float* transform) {
+  if (!path || rows < 0 || cols < 0 || ((size_t)rows * cols && !xyz)) return MR_E_INVALID;
+  M4 xf = identity();
+  if (transform) memcpy(xf.m, transform, sizeof xf.m);
+  FILE* f = fopen(path, "w");
+  if (!f) return MR_E_IO;
+  bool ok = true;
+  const size_t n = (size_t)rows * cols;
+  for (size_t i = 0; i < n && ok; i++) {
+    const float* q = xyz + 3 * i;
+    if (q[2] < -1e-5f) {
+      const F3 p = affine(xf.m, F3{q[0], q[1], q[2]});
+      ok = fprintf(f, "%f %f %f\n", p.x, p.y, p.z) > 0;
+    }
+  }
+  ok = fclose(f) == 0 && ok;
+  return ok ? MR_OK : MR_E_IO;
+}
+
 }  // extern "C"

@@ -89,6 +89,18 @@ def save_ppm(path: str, rgb8: np.ndarray) -> None:
     _check(capi.lib().mr_ppm_save(path.encode(), a.ctypes.data, a.shape[0], a.shape[1]), f"mr_ppm_save({path})")
 
 
+def save_xyz(path: str, points: np.ndarray, transform: Optional[np.ndarray] = None) -> None:
+    """saveXYZ: the points (rows, cols, 3) with z < -1e-5 (a range image's
+    covered pixels) as "x y z" text lines, after `transform` (default the
+    identity)."""
+    a = np.ascontiguousarray(points, np.float32)
+    if a.ndim != 3 or a.shape[2] != 3:
+        raise ValueError("points must be (rows, cols, 3)")
+    xf = None if transform is None else np.ascontiguousarray(transform, np.float32).reshape(4, 4)
+    _check(capi.lib().mr_xyz_save(path.encode(), a.ctypes.data, a.shape[0], a.shape[1],
+                                  None if xf is None else xf.ctypes.data), f"mr_xyz_save({path})")
+
+
 def save_stl(path: str, mesh: TriMesh, transform: Optional[np.ndarray] = None) -> None:
     """saveSTL: binary STL of the mesh's triangles under `transform`
     (default: the mesh's own transform, as the reference uses)."""

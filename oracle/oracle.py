@@ -102,6 +102,7 @@ def ref_lib() -> Optional[C.CDLL]:
         L.ref_ppm_load.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.ref_ppm_save.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32]
         L.ref_stl_save.argtypes = [C.c_char_p, C.c_void_p, C.c_void_p]
+        L.ref_xyz_save.argtypes = [C.c_char_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]
         L.ref_paint.restype = C.c_int
         L.ref_paint.argtypes = [C.POINTER(abi.mr_frame), C.c_void_p, C.c_int32, C.c_void_p, C.c_int32, C.c_int,
                                 C.c_int32] + [C.c_void_p] * 8
@@ -159,6 +160,13 @@ def ref_save_ppm(path: str, rgb: np.ndarray) -> None:
     """The reference's savePPM of a float image (rows, cols, 3)."""
     a = np.ascontiguousarray(rgb, np.float32)
     ref_lib().ref_ppm_save(path.encode(), _ptr(a), a.shape[0], a.shape[1])
+
+
+def ref_save_xyz(path: str, points: np.ndarray, transform=None) -> None:
+    """The reference's saveXYZ of a (rows, cols, 3) float image."""
+    a = np.ascontiguousarray(points, np.float32)
+    xf = None if transform is None else np.ascontiguousarray(transform, np.float32)
+    ref_lib().ref_xyz_save(path.encode(), _ptr(a), a.shape[0], a.shape[1], None if xf is None else _ptr(xf))
 
 
 def ref_save_stl(path: str, desc, transform=None) -> None:

@@ -299,6 +299,16 @@ void ref_ppm_save(const char* path, const float* rgb, int32_t rows, int32_t cols
     }
   savePPM(t, path);
 }
+void ref_xyz_save(const char* path, const float* xyz, int32_t rows, int32_t cols, const float* transform) {
+  Array2<Vec3> t(rows, cols);
+  for (int r = 0; r < rows; r++)
+    for (int c = 0; c < cols; c++) {
+      const float* v = xyz + 3 * ((size_t)r * cols + c);
+      t(r, c) = Vec3(v[0], v[1], v[2]);
+    }
+  if (transform) saveXYZ(t, path, to_m4(transform));
+  else saveXYZ(t, path);
+}
 void ref_stl_save(const char* path, const mr_mesh_desc* d, const float* transform) {
   Shared<TriMesh> m = make_mesh(*d);
   if (transform) m->transform = to_m4(transform);

@@ -170,6 +170,34 @@ def test_stl_save_matches_reference(tmp_path, product_lib, ref_lib):
     assert open(a, "rb").read() == open(b, "rb").read()
 
 
+def test_xyz_save_matches_reference(tmp_path, product_lib, ref_lib):
+    """saveXYZ of a range image and of points around the z < -1e-5 cut,
+    with the identity and with a transform: the same text as the
+    reference's own saveXYZ."""
+    st, sc = W.config1(64, 48)
+    rng_img = O.range_image(st, O.render(st, sc)["depth"])
+    rng = np.random.default_rng(12)
+    pts = rng.normal(size=(9, 13, 3)).astype(np.float32)
+    pts[0, :4, 2] = np.float32([-1e-5, -1.0001e-5, 0.0, -0.0])  # exactly at, just past, zero, negative zero
+    xf = np.array([[0.5, 0, 0.1, 1], [0, 2, 0, -1], [0.3, 0, 1, 0.25], [0, 0, 0, 1]], np.float32)
+    for k, (img, m) in enumerate([(rng_img, None), (rng_img, xf), (pts, None), (pts, xf)]):
+        a, b = str(tmp_path / f"ref{k}.xyz"), str(tmp_path / f"gpu{k}.xyz")
+        O.ref_save_xyz(a, img, m)
+        loaders.save_xyz(b, img, m)
+        assert open(a, "rb").read() == open(b, "rb").read(), k
+    assert len(open(str(tmp_path / "gpu0.xyz")).read().splitlines()) == int((rng_img[..., 2] < -1e-5).sum()) > 100
+
+
+def test_xyz_save_rejects_bad_arguments(tmp_path, product_lib):
+    L = capi.lib()
+    p = str(tmp_path / "x.xyz").encode()
+    assert L.mr_xyz_save(None, None, 0, 0, None) == abi.MR_E_INVALID
+    assert L.mr_xyz_save(p, None, -1, 3, None) == abi.MR_E_INVALID
+    assert L.mr_xyz_save(p, None, 2, 3, None) == abi.MR_E_INVALID
+    assert L.mr_xyz_save(p, None, 0, 3, None) == abi.MR_OK  # empty image, empty file
+    assert os.path.getsize(p.decode()) == 0
+
+
 def test_large_files_parsed_in_parallel_match_reference(tmp_path, product_lib, ref_lib):
     """Binary STL above 200k facets and OBJ above 4 MB take the multi-threaded
     paths; the result is the same as the reference's serial parse."""
