@@ -23,6 +23,9 @@
 //   grow NODE T    appends one triangle (a copy of triangle T, pushed 0.5
 //                  along +z) to the node's mesh: the arrays are reallocated
 //                  and longer, which the binding must notice
+//   detach NODE  removes the node from its parent's children (the binding
+//                frees the meshes the next frame does not use)
+//   attach NODE  appends it to its parent's children again
 //   out PREFIX   -> PREFIX.image/.depth/.rgb8/.ids/.range[/.normals]
 // Exit status 3 with the message on stdout when the binding throws GpuError.
 #include <stdio.h>
@@ -123,6 +126,7 @@ int run(const char* scene_file) {
   std::vector<MeshData> meshes;
   std::vector<asl::Array2<asl::Vec3>> textures;
   std::vector<asl::Shared<SceneNode>> nodes;
+  std::vector<int> parents;
   std::vector<asl::Shared<TriMesh>> painted;  // paintMesh meshes stay alive until exit
   asl::Shared<Scene> scene;
   bool save_normals = false, scene_set = false;
@@ -200,6 +204,7 @@ int run(const char* scene_file) {
       node->transform = read_matrix(in);
       if (parent >= 0) nodes[parent]->children << node;
       nodes.push_back(node);
+      parents.push_back(parent);
     } else if (cmd == "ambient") {
       in >> scene->ambientLight;
     } else if (cmd == "render") {
@@ -255,6 +260,20 @@ int run(const char* scene_file) {
         m->indices << nv + c;
         m->normalsI << nn + c;
         if (nt && m->texcoordsI.length()) m->texcoordsI << nt + c;
+      }
+    } else if (cmd == "detach" || cmd == "attach") {
+      int k;
+      in >> k;
+      if (k <= 0 || k >= (int)nodes.size()) throw std::runtime_error(cmd + ": no such node");
+      asl::Array<asl::Shared<SceneNode>>& children = nodes[parents[k]]->children;
+      if (cmd == "attach") {
+        children << nodes[k];
+      } else {
+        asl::Array<asl::Shared<SceneNode>> keep;
+        for (int i = 0; i < children.length(); i++)
+          if (children[i].operator->() != nodes[k].operator->()) keep << children[i];
+        children.clear();
+        for (int i = 0; i < keep.length(); i++) children << keep[i];
       }
     } else if (cmd == "out") {
       std::string prefix;

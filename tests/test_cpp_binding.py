@@ -314,3 +314,36 @@ def test_binding_notices_mesh_edits(product_lib, tmp_path):
         if previous is not None:
             assert not np.array_equal(got["ids"], previous), f"frame {tag} did not change"
         previous = got["ids"]
+
+
+@pytest.mark.gpu
+def test_binding_frees_meshes_the_frame_drops(product_lib, tmp_path):
+    """A node detached from the scene: the next frame no longer draws its
+    mesh (the binding frees it); attached again, the mesh is sent again and
+    drawn -- every frame equals the oracle's render of the scene as it is."""
+    import edge_scenes as E
+    from minirender_gb300.scene import Scene
+    st, sc1 = W.config1(160, 120)
+    sphere = sc1.children[0]
+    cube = E._tri_mesh([[-1.2, -1.2, 0.3], [-0.2, -1.2, 0.3], [-0.2, -0.2, 0.3], [-1.2, -0.2, 0.3]],
+                       [0, 1, 2, 0, 2, 3], material=sphere.material)
+    full = Scene()
+    full.add(sphere)
+    full.add(cube)
+    alone = Scene()
+    alone.add(sphere)
+    exe = build_driver(str(tmp_path))
+    w = SceneWriter(str(tmp_path))
+    w.state(st)
+    w.scene(full)  # node 0 the scene, 1 the sphere, 2 the quad
+    w.lines += ["render", f"out {tmp_path}/a", "detach 2", "render", f"out {tmp_path}/b",
+                "attach 2", "render", f"out {tmp_path}/c"]
+    r = run_driver(exe, w.write())
+    assert r.returncode == 0, r.stdout + r.stderr
+    frames = {}
+    for tag, sc in (("a", full), ("b", alone), ("c", full)):
+        got = read_outputs(f"{tmp_path}/{tag}", st)
+        assert_parity(compare(got, O.render(st, sc), f"cpp_binding_detach_{tag}"))
+        frames[tag] = got["ids"]
+    assert not np.array_equal(frames["a"], frames["b"])
+    assert np.array_equal(frames["a"], frames["c"])
