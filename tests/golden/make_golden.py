@@ -55,7 +55,10 @@ def paint_digests():
     """tests/golden/paints.json: digests of the reference Renderer's image and
     depth for the paintMesh / paintTriangle sequence of
     tests/edge_scenes.paint_sequence, after render() and after clear(), and
-    for the seeded random sequences of tests/edge_scenes.random_paints."""
+    for the seeded random sequences of tests/edge_scenes.random_paints, and
+    for the paints around setView / setLighting / setTexturing / setLight /
+    setBackground calls of tests/edge_scenes.view_change_paints and
+    state_change_paints."""
     import hashlib
     import json
     st, paints = E.paint_sequence()
@@ -66,6 +69,10 @@ def paint_digests():
     for seed in range(8):  # tests/edge_scenes.random_paints, after clear()
         r = O.ref_paint(*E.random_paints(seed), clear=True)
         out[f"random/{seed}"] = {k: hashlib.sha256(r[k].tobytes()).hexdigest() for k in ("image", "depth")}
+    for name, make in (("view_change", E.view_change_paints), ("state_changes", E.state_change_paints)):
+        st, calls, _ = make()
+        r = O.ref_paint(st, calls)
+        out[name] = {k: hashlib.sha256(r[k].tobytes()).hexdigest() for k in ("image", "depth")}
     with open(os.path.join(HERE, "paints.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print("paints.json:", ", ".join(sorted(out)))

@@ -220,6 +220,23 @@ def test_random_paints_vs_reference(ref_lib, seed):
         assert _bits_equal(got["image"], ref["image"]), clear
 
 
+@pytest.mark.parametrize("name", ["view_change", "state_changes"])
+def test_state_paints_match_golden(name):
+    """Paints around setView / setLighting / setTexturing / setLight /
+    setBackground: the oracle's one-list form against the committed digests
+    of the reference's Renderer (tests/golden/paints.json)."""
+    import hashlib
+    import json
+    import edge_scenes as E
+    with open(os.path.join(GOLDEN, "paints.json")) as f:
+        want = json.load(f)[name]
+    make = E.view_change_paints if name == "view_change" else E.state_change_paints
+    st, _, paints = make()
+    got = O.render_paints(st, paints)
+    for k in ("image", "depth"):
+        assert hashlib.sha256(got[k].tobytes()).hexdigest() == want[k], k
+
+
 @pytest.mark.parametrize("seed", range(8))
 def test_random_paints_match_golden(seed):
     """Random paint sequences against the committed digests of the
