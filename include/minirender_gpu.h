@@ -349,7 +349,9 @@ MR_API int mr_server_destroy(mr_server* srv);
  * and the device-wide synchronisation cudaFree implies.  Renders one mesh
  * (one renderable of Renderer::render, src/Renderer.cpp:311-381) with every
  * piece of working memory -- visibility buffer, counters, per-triangle
- * index-check mask, renderable record and triangle-base table -- taken from one
+ * index-check mask, renderable record, triangle-base table and a fixed store
+ * of large-triangle records (32768; further large triangles are rasterised
+ * by the setup kernel, as small ones are) -- taken from one
  * file-scope device array of MR_NOALLOC_SCRATCH_BYTES that the library
  * reserves on each GPU it is loaded on, until the process exits.
  *
@@ -372,7 +374,7 @@ MR_API int mr_server_destroy(mr_server* srv);
  * scratch array, which keeps the previous call's contents: calls whose GPU
  * work overlaps (other host threads, other streams) race on it and must be
  * serialised by the caller. */
-#define MR_NOALLOC_SCRATCH_BYTES (17u << 20)
+#define MR_NOALLOC_SCRATCH_BYTES (20u << 20)
 #define MR_NOALLOC_MAX_SIDE 4096
 #define MR_NOALLOC_MAX_PIXELS (1 << 21)
 #define MR_NOALLOC_MAX_TRIANGLES (1 << 22)

@@ -886,6 +886,8 @@ __global__ void __launch_bounds__(kSetupThreads, kSetupMinBlocks<PRE>) k_setup(F
       if (slot < F.rec_cap) {
         F.recs[slot] = to_rec(S[s], 2u * g + (uint32_t)s);
         n_items = (unsigned)(S[s].y1 - S[s].y0 + kLargeRows) / kLargeRows;
+      } else {
+        kind[s] = 1;  // no record left (a fixed record store): rasterised below
       }
     }
     // its row blocks: one range per warp, each lane's at its exclusive prefix

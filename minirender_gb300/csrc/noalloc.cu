@@ -15,7 +15,9 @@
 // Every call shares the array and inherits the previous call's contents, so
 // the counters are cleared each call; the visibility buffer is cleared by the
 // frame's own clear kernel and the index mask is rewritten by the validation
-// kernel.  Calls whose GPU work overlaps race on the array.
+// kernel.  Large sub-triangles get records and row blocks in the array as in
+// mr_render, up to kRecCap of them; any further ones are rasterised by the
+// setup kernel itself.  Calls whose GPU work overlaps race on the array.
 #include <cuda_runtime.h>
 #include <string.h>
 
@@ -33,7 +35,12 @@ constexpr size_t kBadBytes = ((size_t)MR_NOALLOC_MAX_TRIANGLES / 32 + 1) * sizeo
 constexpr size_t kCntOff = al(kBadOff + kBadBytes);
 constexpr size_t kRsOff = al(kCntOff + sizeof(Counters));
 constexpr size_t kBaseOff = al(kRsOff + sizeof(DevRenderable));
-constexpr size_t kEnd = al(kBaseOff + 2 * sizeof(uint32_t));
+constexpr uint32_t kRecCap = 1u << 15;   // large sub-triangles with a record
+constexpr uint32_t kItemCap = 1u << 16;  // their 32-row blocks (more: the spill list)
+constexpr size_t kRecOff = al(kBaseOff + 2 * sizeof(uint32_t));
+constexpr size_t kItemOff = al(kRecOff + (size_t)kRecCap * sizeof(BigRec));
+constexpr size_t kSpillOff = al(kItemOff + (size_t)kItemCap * sizeof(LargeItem));
+constexpr size_t kEnd = al(kSpillOff + (size_t)kRecCap * sizeof(LargeItem));  // one entry per record at most
 static_assert(kEnd <= MR_NOALLOC_SCRATCH_BYTES, "scratch layout exceeds MR_NOALLOC_SCRATCH_BYTES");
 
 }  // namespace
@@ -141,17 +148,18 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   memcpy(F.v.bg, f->background, sizeof(F.v.bg));
   F.g.n_renderables = 1;
   F.g.n_tris = (uint32_t)M.n_tri;
-  // Every sub-triangle is rasterised by the setup kernel itself, so no
-  // (data-dependent) record or row-block storage is needed.
-  F.small_max = 0x7fffffff;
+  // Sub-triangles up to 64 pixels of bounding box are rasterised by the setup
+  // kernel; larger ones take records and row blocks from the fixed store
+  // (the spill list holds one entry per record, so it cannot overflow).
+  F.small_max = 64;
   F.g.rs = (const DevRenderable*)(S + kRsOff);
   F.g.tri_base = (const uint32_t*)(S + kBaseOff);
   F.vis = (unsigned long long*)(S + kVisOff);
-  F.recs = nullptr;
-  F.rec_cap = 0;
-  F.items = nullptr;
-  F.item_cap = 0;
-  F.spill = nullptr;
+  F.recs = (BigRec*)(S + kRecOff);
+  F.rec_cap = kRecCap;
+  F.items = (LargeItem*)(S + kItemOff);
+  F.item_cap = kItemCap;
+  F.spill = (LargeItem*)(S + kSpillOff);
   F.rgb8 = rgb8;
   F.depth = depth;
   F.ids = tri_id;

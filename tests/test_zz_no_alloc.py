@@ -109,6 +109,43 @@ def test_noalloc_matches_existing_entry_point(product_lib, name, case):
         _same(got, ref, f"call {k} vs the oracle")
 
 
+def _strips(n, w, h, seed):
+    """n thin horizontal triangles of 80-200 x 3 pixels (each bounding box
+    above 64 pixels, so each one takes a large-triangle record), front-facing,
+    at random depths, under an orthographic projection of one unit per pixel."""
+    from minirender_gb300 import projection as pj
+    from minirender_gb300.frame import FrameState
+    rng = np.random.default_rng(seed)
+    x0 = rng.uniform(-w / 2, w / 2 - 200, n)
+    y0 = rng.uniform(-h / 2, h / 2 - 3, n)
+    ln = rng.uniform(80, 200, n)
+    z = -rng.uniform(2, 50, n)
+    v = np.stack([np.stack([x0, y0, z], 1), np.stack([x0 + ln, y0 + 0.5, z], 1),
+                  np.stack([x0, y0 + 2, z], 1)], 1).reshape(-1, 3).astype(np.float32)
+    idx = np.arange(3 * n, dtype=np.int32)
+    nrm = np.tile(np.array([[0.2, 0.3, 1]], np.float32), (3 * n, 1))
+    sc = S.Scene()
+    sc.add(S.TriMesh(v, nrm, idx, normalsI=idx, material=S.Material(diffuse=(0.3, 0.8, 0.5), shininess=12)))
+    st = FrameState(width=w, height=h, projection=pj.projection_ortho(-w / 2, w / 2, -h / 2, h / 2, 1, 60),
+                    light=np.array([0.3, 0.4, 1], np.float32))
+    return st, sc
+
+
+@pytest.mark.parametrize("case", ["big_triangles", "strips_past_the_record_store"])
+def test_noalloc_large_triangles(product_lib, case):
+    """Large sub-triangles take records from the fixed store and the
+    row-parallel raster kernel; past the store's 32768 records the setup
+    kernel rasterises them itself. Both equal the oracle and mr_render."""
+    import edge_scenes as E
+    st, sc = E.ALL["big_triangles"]() if case == "big_triangles" else _strips(40000, 1024, 768, 5)
+    want = _existing(st, sc)
+    ref = O.render(st, sc)
+    assert (ref["ids"] != 0xFFFFFFFF).sum() > 10000
+    for k, got in enumerate(_noalloc(st, sc)):
+        _same(got, want, f"call {k} vs mr_render")
+        _same(got, ref, f"call {k} vs the oracle")
+
+
 def test_noalloc_bad_index_then_good_mesh(product_lib):
     """One out-of-range index (found by the index check, which reads only the
     caller's in-bounds index memory) gives MR_E_BAD_INDEX; the next call with
