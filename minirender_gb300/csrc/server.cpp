@@ -499,7 +499,9 @@ MR_API int mr_server_create(mr_ctx* c, const mr_server_opts* o, mr_server** out)
 
 MR_API int mr_server_submit(mr_server* s, const mr_request* q, uint64_t* ticket) {
   if (!s || !q || !ticket) return MR_E_INVALID;
-  if (q->frame.width <= 0 || q->frame.height <= 0 || q->mesh.n_indices % 3 || q->mesh.n_indices < 0 ||
+  // the mesh descriptor is checked as every entry point checks it (negative
+  // counts would otherwise reach the footprint arithmetic below)
+  if (q->frame.width <= 0 || q->frame.height <= 0 || mesh_desc_problem(&q->mesh) ||
       (q->texture_key && (!q->texture_rgb8 || q->tex_rows <= 0 || q->tex_cols <= 0)))
     return MR_E_INVALID;
   Request* r = new Request();

@@ -163,6 +163,40 @@ def test_server_empty_mesh_request(ctx):
         srv.close()
 
 
+def test_server_rejects_bad_mesh_descriptors(ctx):
+    """Descriptors that mr_mesh_upload refuses (negative counts, a null array
+    with a non-zero count, normalsI shorter than indices) are refused at
+    submit with MR_E_INVALID, before any queueing; a good request after them
+    completes."""
+    import ctypes as C
+    from minirender_gb300.server import RenderServer
+    st, sc = W.config1(64, 48)
+    m = sc.children[0]
+    srv = RenderServer(ctx, budget_bytes=1 << 30, slots=1, max_batch=4)
+    try:
+        good = m.desc()
+        bad = []
+        for field, value in (("n_vertices", -3), ("vertices", None), ("n_normalsI", 3)):
+            d = m.desc()
+            setattr(d, field, value)
+            bad.append(d)
+        for d in bad:
+            q = abi.mr_request()
+            q.frame = st.to_c()
+            q.mesh_key = 7
+            q.mesh = d
+            q.transform[:] = [float(x) for x in np.eye(4, dtype=np.float32).reshape(16)]
+            ticket = C.c_uint64(0)
+            assert capi.lib().mr_server_submit(srv.h, C.byref(q), C.byref(ticket)) == abi.MR_E_INVALID
+        assert good.n_vertices > 0
+        out = _buffers(st)
+        t = srv.submit(st, m, mesh_key=8, out=out)
+        assert srv.wait(t).status == 0
+        assert _same(out, _oracle(st, m))
+    finally:
+        srv.close()
+
+
 def _random_requests(n=48):
     """First mesh of each seeded random scene (soup or indexed, clipped, both
     projections, odd frame sizes), with its node transform and an RGB8
