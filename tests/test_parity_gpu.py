@@ -200,6 +200,30 @@ def test_paint_mesh_and_triangles(renderer, clear):
     assert stats["covered"] > 5000
 
 
+@pytest.mark.parametrize("seed", range(32))
+def test_random_paints(renderer, seed):
+    """Seeded random paintMesh / paintTriangle sequences after render() and
+    clear() (tests/edge_scenes.random_paints: new transforms and materials,
+    RGB8 textures, clipped and unclipped view-space triangles, both
+    projections), pinned to the reference's Renderer on the CPU: the mirror
+    on GB300 equals the oracle."""
+    import copy
+    from minirender_gb300.scene import Scene
+    st, paints = E.random_paints(seed)
+    renderer.state = copy.deepcopy(st)
+    empty = Scene()
+    empty.ambientLight = st.ambient  # render() takes the scene's ambient, as the reference does
+    renderer.setScene(empty)
+    renderer.render()
+    renderer.clear()
+    _replay_paints(renderer, paints)
+    gpu = {"image": renderer.getImage(), "depth": renderer.getDepth(), "ids": renderer.getTriangleIds(),
+           "rgb8": renderer.getImageRGB8()}
+    stats = compare(gpu, O.render_paints(st, paints), f"random_paints_{seed}")
+    report(stats)
+    assert_parity(stats)
+
+
 def test_paint_after_view_change(renderer):
     """render() of a scene, paintMesh, setView, then more paintMesh and a
     paintTriangle run: the later meshes take the new view, the light stays
