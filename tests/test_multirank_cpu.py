@@ -62,3 +62,17 @@ def test_reference_arm_under_torchrun():
         assert k in d, k
     assert d["steps"] == 1 and d["warmup"] == 3 and d["metric"] == d["unit"] == "frames/s"
     assert d["config"]["workload"] and d["cpu_baseline"]["cores"] >= 1 and d["cpu_baseline"]["sample"]
+
+
+def test_serving_rows_take_the_median_stream():
+    """bench.py's served rows: with several streams per row the reported one
+    is the median by frames/s (the lower middle one for an even count), and
+    every stream's rate is listed; one stream is reported as it is."""
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    import bench
+    runs = [{"frames_per_s": 5.0, "p99_ms": 1}, {"frames_per_s": 3.0, "p99_ms": 2}, {"frames_per_s": 9.0, "p99_ms": 3}]
+    row = bench._median_run(runs)
+    assert row["frames_per_s"] == 5.0 and row["p99_ms"] == 1
+    assert row["streams"] == 3 and row["frames_per_s_each"] == [5.0, 3.0, 9.0]
+    assert bench._median_run(runs[:2])["frames_per_s"] == 3.0
+    assert bench._median_run(runs[:1]) == runs[0]
