@@ -696,12 +696,9 @@ MR_API int mr_render(mr_ctx* c, const mr_frame* f, const mr_renderable* rs, int3
   F.v.persp = f->projection[15] == 0;
   float zn = F.v.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
   F.v.znear = -zn;
-  F.v.point = f->light_is_point != 0;
-  if (F.v.point) affine(f->view, f->light, F.v.lightdir);
+  if (f->light_is_point) affine(f->view, f->light, F.v.lightdir);
   else normalized(f->light, F.v.lightdir);
   F.v.ambient = f->ambient;
-  F.v.lighting = f->lighting != 0;
-  F.v.save_normals = f->save_normals != 0;
   memcpy(F.v.bg, f->background, sizeof(F.v.bg));
   F.g.n_renderables = n;
   F.g.n_tris = (uint32_t)total;
@@ -890,12 +887,9 @@ static void make_view(const mr_frame* f, View& V) {
   V.persp = f->projection[15] == 0;
   float zn = V.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
   V.znear = -zn;
-  V.point = f->light_is_point != 0;
-  if (V.point) affine(f->view, f->light, V.lightdir);
+  if (f->light_is_point) affine(f->view, f->light, V.lightdir);
   else normalized(f->light, V.lightdir);
   V.ambient = f->ambient;
-  V.lighting = f->lighting != 0;
-  V.save_normals = f->save_normals != 0;
   memcpy(V.bg, f->background, sizeof(V.bg));
 }
 

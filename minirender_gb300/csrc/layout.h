@@ -66,10 +66,8 @@ struct View {
   float P[16];
   int persp;
   float znear;
-  float lightdir[3];
-  int point;
+  float lightdir[3];  // placed as render() places it (src/Renderer.cpp:317-320)
   float ambient;
-  int lighting, save_normals;
   float bg[3];
 };
 

@@ -140,11 +140,9 @@ extern "C" MR_API int mr_render_noalloc(const mr_frame* f, const mr_mesh_desc* d
   F.v.persp = f->projection[15] == 0;
   float zn = F.v.persp ? f->projection[11] / (f->projection[10] - 1) : (f->projection[11] + 1) / f->projection[10];
   F.v.znear = -zn;
-  F.v.point = f->light_is_point != 0;
-  if (F.v.point) affine(f->view, f->light, F.v.lightdir);
+  if (f->light_is_point) affine(f->view, f->light, F.v.lightdir);
   else normalized(f->light, F.v.lightdir);
   F.v.ambient = f->ambient;
-  F.v.lighting = f->lighting != 0;
   memcpy(F.v.bg, f->background, sizeof(F.v.bg));
   F.g.n_renderables = 1;
   F.g.n_tris = (uint32_t)M.n_tri;
