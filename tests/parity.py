@@ -109,9 +109,10 @@ def summary_markdown(report_dir: str, result: str = "") -> str:
 
     out = ["# Parity on GB300: every GPU case against the oracle", "",
            "Command (one GB300, the repository as committed):", "", "```",
+           "DIR=parity_reports",
            'python -c "import __graft_entry__ as g; g.build()" && \\',
-           "MR_PARITY_REPORT_DIR=gpurun_out/parity python -m pytest tests -m gpu -q && \\",
-           "python tests/parity.py gpurun_out/parity > profiles/parity_all_cases.md", "```", ""]
+           "MR_PARITY_REPORT_DIR=$DIR python -m pytest tests -m gpu -q && \\",
+           "python tests/parity.py $DIR > profiles/parity_all_cases.md", "```", ""]
     if result:
         out += [f"Result: {result}.", ""]
     out += ["The parity tests write one line per compared frame into `$MR_PARITY_REPORT_DIR` (plain path and",
@@ -159,4 +160,6 @@ if __name__ == "__main__":
         i = args.index("--result")
         res = args[i + 1]
         del args[i:i + 2]
-    sys.stdout.write(summary_markdown(args[0] if args else "gpurun_out/parity", res))
+    if len(args) != 1:
+        sys.exit("usage: python tests/parity.py REPORT_DIR [--result TEXT] > profiles/parity_all_cases.md")
+    sys.stdout.write(summary_markdown(args[0], res))
