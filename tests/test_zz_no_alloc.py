@@ -4,7 +4,9 @@ cannot pay for cudaMalloc/cudaFree).  It keeps its working memory in a fixed
 device array inside the library, so this test checks that its output equals
 the ordinary entry point's (mr_render through Renderer) and the oracle's on
 two calls in a row -- the second call starts from the scratch the first one
-left behind -- for an untextured and a textured scene; that a mesh with an
+left behind -- for an untextured and a textured scene, for large triangles
+(records from the fixed store) and for more large triangles than the store
+holds (the rest rasterised by the setup kernel); that a mesh with an
 out-of-range index is reported and a good mesh right after it renders
 correctly (no stale index-check bits); that an empty mesh with no outputs
 succeeds; and that oversized requests are refused before any device work.
