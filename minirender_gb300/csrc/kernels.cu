@@ -493,22 +493,6 @@ __device__ __forceinline__ void shade(const View& V, const DevRenderable& R, con
   }
 }
 
-// Depth terms of the winning sub-triangle's corners: the values its setup
-// used (src/Renderer.cpp:223-224).
-template <bool PRE>
-__device__ __forceinline__ void winner_zterms(const View& V, const Geo& G, const DevRenderable& R,
-                                              const int (&ip)[3], const Vtx (&vc)[3], bool clipped,
-                                              float (&zt)[3]) {
-  if (PRE && !clipped) {
-#pragma unroll
-    for (int c = 0; c < 3; c++) zt[c] = G.va[R.vert_base + ip[c]].z;
-  } else {
-    float px, py;
-#pragma unroll
-    for (int c = 0; c < 3; c++) project(V, vc[c].pos, px, py, zt[c]);
-  }
-}
-
 // The setup (src/Renderer.cpp:198-224) of the winning sub-triangle, the same
 // values its raster used.
 template <bool PRE>
@@ -1388,12 +1372,11 @@ __global__ void __launch_bounds__(256, MINB) k_batch(BatchParams B, uint32_t* bl
         Setup S;
         float e1, e2;
         const float2 ee = captured ? s_e[i] : make_float2(__int_as_float(0x7fc00000), 0.f);
+        winner_setup<PRE>(s_view, B.g, R, ip, vc, clipped, S);
         if (ee.x == ee.x) {  // won by a record of this tile: edge values captured
-          winner_zterms<PRE>(s_view, B.g, R, ip, vc, clipped, S.z);
           e1 = ee.x;
           e2 = ee.y;
         } else {  // won by a small triangle rasterised in the setup kernel
-          winner_setup<PRE>(s_view, B.g, R, ip, vc, clipped, S);
           replay(S, x, y, e1, e2);
         }
         float k0, k1, k2;
